@@ -1,0 +1,318 @@
+"""Generate golden vectors by running the TORCH reference itself.
+
+Run in a container that has the reference source tree (default
+``/root/reference``, or ``$TORCH_REFERENCE``):
+
+    python tests/golden/make_golden.py
+
+The reference package ``cfdSolver`` imports matplotlib at package level, so it
+is loaded through a bare namespace module whose ``__path__`` points at the
+source directory; the solver modules themselves need only NumPy.  Every case
+uses small seeded inputs.  Outputs go to ``tests/golden/*.npz`` next to this
+script and are committed; tests read them without the reference.
+"""
+
+import os
+import sys
+import types
+import importlib
+from pathlib import Path
+
+import numpy as np
+
+OUT = Path(__file__).resolve().parent
+REF = Path(os.environ.get("TORCH_REFERENCE", "/root/reference")) / "python"
+
+
+def load_reference():
+    pkg = types.ModuleType("cfdSolver")
+    pkg.__path__ = [str(REF / "cfdSolver")]
+    sys.modules["cfdSolver"] = pkg
+    names = ("torchSolver", "torchSolver2D", "torchSolver3D", "torchFlux",
+             "torchSession", "torchExecution")
+    return types.SimpleNamespace(**{n: importlib.import_module("cfdSolver." + n)
+                                    for n in names})
+
+
+LIMITERS = ("VanLeer", "Albada", "MINBEE", "Superbee", "Unos")
+
+
+def blob_primitive(rng, dim, shape, jump=True):
+    """Seeded smooth field plus a discontinuous blob, positive rho and p."""
+    coords = np.meshgrid(*[(np.arange(n) + 0.5) / n for n in shape], indexing="ij")
+    r2 = sum((c - 0.45) ** 2 for c in coords)
+    p = np.empty((dim + 2,) + shape)
+    p[0] = 1.0 + 0.3 * rng.random(shape)
+    for m in range(1, dim + 1):
+        p[m] = 0.4 * (rng.random(shape) - 0.5)
+    p[-1] = 1.0 + 0.3 * rng.random(shape)
+    if jump:
+        inside = r2 <= 0.3 ** 2
+        p[0] = np.where(inside, p[0] * 4.0, p[0])
+        p[-1] = np.where(inside, p[-1] * 6.0, p[-1])
+    return p
+
+
+def hllc_cases(R, rng):
+    out = {}
+    for nv in (4, 5):
+        n = 1500
+        p_l = np.empty((nv, n))
+        p_r = np.empty((nv, n))
+        for p in (p_l, p_r):
+            p[0] = 0.05 + 3 * rng.random(n)
+            p[1:-1] = 4 * (rng.random((nv - 2, n)) - 0.5)
+            p[-1] = 0.01 + 5 * rng.random(n)
+        # identical states, contacts and strong shocks
+        p_r[:, :100] = p_l[:, :100]
+        p_r[1, 100:200] = p_l[1, 100:200]
+        p_r[-1, 100:200] = p_l[-1, 100:200]
+        p_l[-1, 200:300] *= 1e4
+        gl = 1.15 + 0.3 * rng.random(n)
+        gr = np.where(rng.random(n) < 0.5, gl, 1.15 + 0.3 * rng.random(n))
+        cons = []
+        for p, g in ((p_l, gl), (p_r, gr)):
+            u = p.copy()
+            u[1:-1] *= p[0]
+            u[-1] = p[-1] / (g - 1) + 0.5 * p[0] * np.sum(p[1:-1] ** 2, axis=0)
+            cons.append(u)
+        out[f"ul{nv}"], out[f"ur{nv}"] = cons
+        out[f"gl{nv}"], out[f"gr{nv}"] = gl, gr
+        out[f"flux{nv}"] = R.torchFlux.hllc_flux(cons[0], cons[1], gl, gamma_right=gr)
+    np.savez_compressed(OUT / "hllc.npz", **out)
+
+
+def step3d_cases(R, rng):
+    out = {}
+    bc_sets = [("Open", "Open", "Open"), ("Reflective", "Periodic", "Open"),
+               ("Periodic", "Reflective", "Reflective")]
+    k = 0
+    for limiter in LIMITERS:
+        for bcs in bc_sets:
+            shape = (5, 6, 7)  # nz, ny, nx
+            prim = blob_primitive(rng, 3, shape)
+            gamma = 1.4 if k % 2 == 0 else 1.2 + 0.2 * rng.random(shape)
+            state = R.torchSolver3D.uprim_to_uconsv_3d(prim, gamma)
+            h = (1 / 7, 1.3 / 6, 0.9 / 5)
+            dt = 0.2 * min(h) / 4.0
+            res, fluxes = R.torchSolver3D._hydro(state, gamma, h, dt, limiter, bcs[::-1])
+            out[f"c{k}_state"] = state
+            out[f"c{k}_gamma"] = np.broadcast_to(gamma, shape).copy()
+            out[f"c{k}_meta"] = np.array([*h, dt])
+            out[f"c{k}_limiter"] = np.array(limiter)
+            out[f"c{k}_bcs"] = np.array(bcs)
+            out[f"c{k}_result"] = res
+            for d, f in enumerate(fluxes):
+                out[f"c{k}_flux{d}"] = f
+            k += 1
+    # rough seeded field: the second-order step is nonphysical, so the whole
+    # step is redone at first order (Rusanov)
+    shape = (4, 4, 6)
+    p = np.empty((5,) + shape)
+    p[0] = 10 ** rng.uniform(-3, 1, shape)
+    p[1:4] = rng.uniform(-3, 3, (3,) + shape)
+    p[4] = 10 ** rng.uniform(-4, 1, shape)
+    state = R.torchSolver3D.uprim_to_uconsv_3d(p)
+    h = (1 / 6, 1 / 4, 1 / 4)
+    q = R.torchSolver3D.uconsv_to_uprim_3d(state)
+    sound = np.sqrt(1.4 * q[4] / q[0])
+    dt = 0.4 / sum(np.max(abs(q[m]) + sound) / d for m, d in enumerate(h, 1))
+    res, fluxes = R.torchSolver3D._hydro(state, 1.4, h, dt, "Superbee",
+                                         ("Reflective", "Periodic", "Open"))
+    out[f"c{k}_state"] = state
+    out[f"c{k}_gamma"] = np.full(state.shape[1:], 1.4)
+    out[f"c{k}_meta"] = np.array([*h, dt])
+    out[f"c{k}_limiter"] = np.array("Superbee")
+    out[f"c{k}_bcs"] = np.array(("Open", "Periodic", "Reflective"))
+    out[f"c{k}_result"] = res
+    for d, f in enumerate(fluxes):
+        out[f"c{k}_flux{d}"] = f
+    out["count"] = np.array(k + 1)
+    np.savez_compressed(OUT / "step3d.npz", **out)
+
+
+def step2d_cases(R, rng):
+    out = {}
+    bc_sets = [("Open", "Open"), ("Reflective", "Periodic"), ("Periodic", "Reflective"),
+               ("Open", "Inflow")]
+    k = 0
+    for limiter in LIMITERS:
+        for bc_x, bc_y in bc_sets:
+            shape = (9, 11)
+            prim = blob_primitive(rng, 2, shape)
+            gamma = 1.4 if k % 2 == 0 else 1.2 + 0.2 * rng.random(shape)
+            state = R.torchSolver2D.uprim_to_uconsv_2d(prim, gamma)
+            dx, dy = 1 / 11, 1.2 / 9
+            dt = 0.05 * min(dx, dy)
+            inlet = [1.1, 0.1, 0.6, 1.3]
+            res, fx, fy = R.torchSolver2D.muscl_hancock_step_2d(
+                state, dx, dy, dt, gamma, limiter, bc_x, bc_y, return_fluxes=True,
+                inlet_primitive=inlet)
+            out[f"c{k}_state"] = state
+            out[f"c{k}_gamma"] = np.broadcast_to(gamma, shape).copy()
+            out[f"c{k}_meta"] = np.array([dx, dy, dt])
+            out[f"c{k}_limiter"] = np.array(limiter)
+            out[f"c{k}_bcs"] = np.array((bc_x, bc_y))
+            out[f"c{k}_inlet"] = np.array(inlet)
+            out[f"c{k}_result"] = res
+            out[f"c{k}_flux0"] = fx
+            out[f"c{k}_flux1"] = fy
+            k += 1
+    # rough seeded field whose second-order update is nonphysical: the step is
+    # redone with the first-order LLF fluxes
+    shape = (6, 8)
+    p = np.empty((4,) + shape)
+    p[0] = 10 ** rng.uniform(-3, 1, shape)
+    p[1:3] = rng.uniform(-3, 3, (2,) + shape)
+    p[3] = 10 ** rng.uniform(-4, 1, shape)
+    state = R.torchSolver2D.uprim_to_uconsv_2d(p, 1.4)
+    dx, dy = 1 / 8, 1 / 6
+    padded = R.torchSolver2D.apply_boundary_conditions_2d(state, "Open", "Reflective")
+    gp = R.torchSolver2D.pad_scalar_2d(np.full(shape, 1.4), "Open", "Reflective", 1.4)
+    dt = R.torchSolver2D.compute_cfl_dt_2d(
+        R.torchSolver2D.uconsv_to_uprim_2d(padded, gp), dx, dy, 0.4, gp)
+    res, fx, fy = R.torchSolver2D.muscl_hancock_step_2d(
+        state, dx, dy, dt, 1.4, "Superbee", "Open", "Reflective", return_fluxes=True)
+    out[f"c{k}_state"] = state
+    out[f"c{k}_gamma"] = np.full(state.shape[1:], 1.4)
+    out[f"c{k}_meta"] = np.array([dx, dy, dt])
+    out[f"c{k}_limiter"] = np.array("Superbee")
+    out[f"c{k}_bcs"] = np.array(("Open", "Reflective"))
+    out[f"c{k}_inlet"] = np.array([1.0, 0.0, 100.0, 101325.0])
+    out[f"c{k}_result"] = res
+    out[f"c{k}_flux0"] = fx
+    out[f"c{k}_flux1"] = fy
+    out["count"] = np.array(k + 1)
+    np.savez_compressed(OUT / "step2d.npz", **out)
+
+
+def chemistry_cases(R, rng):
+    out = {}
+    n = 500
+    for model in ("arrhenius", "znd"):
+        lam = rng.random(n)
+        beta = rng.random(n)
+        rho = 0.5 + rng.random(n)
+        u = 100 * (rng.random(n) - 0.5)
+        p = 101325 * (1 + 40 * rng.random(n))
+        g = R.torchSolver.gamma_calc(lam)
+        state = np.vstack((rho, rho * u, p / (g - 1) + 0.5 * rho * u * u))
+        dt = 2e-6
+        lam_new, st, beta_new = R.torchSolver.new_lambda_n_e_calc(lam, dt, state, model, beta)
+        out[f"{model}_lam"], out[f"{model}_beta"], out[f"{model}_state"] = lam, beta, state
+        out[f"{model}_out_lam"], out[f"{model}_out_state"] = lam_new, st
+        out[f"{model}_out_beta"] = beta_new
+    out["dt"] = np.array(2e-6)
+    # 3D reaction step
+    shape = (3, 4, 5)
+    prim = np.empty((5,) + shape)
+    prim[0] = 0.5 + rng.random(shape)
+    prim[1:4] = 50 * (rng.random((3,) + shape) - 0.5)
+    prim[4] = 101325 * (1 + 20 * rng.random(shape))
+    lam = rng.random(shape)
+    beta = rng.random(shape)
+    state = R.torchSolver3D.uprim_to_uconsv_3d(prim, R.torchSolver.gamma_calc(lam))
+    res, l3, b3 = R.torchSolver3D.reaction_step_3d(state, lam, beta, 3e-6, "znd")
+    out.update(r3_state=state, r3_lam=lam, r3_beta=beta, r3_out=res, r3_out_lam=l3,
+               r3_out_beta=b3)
+    np.savez_compressed(OUT / "chemistry.npz", **out)
+
+
+def session_cases(R, rng):
+    """Multi-step Simulation.step() trajectories (state, time, integrals)."""
+    S = R.torchSession.Simulation
+    out = {}
+    cases = {}
+    cases["s2d_explosion"] = S.preset("2d_explosion", [24, 20], t_end=0.05,
+                                      limiter="VanLeer")
+    p3 = R.torchSolver3D.get_3d_preset("3d_explosion", 10, 9, 8)["primitive"]
+    cases["s3d_explosion"] = S(p3, [1, 1, 1], t_end=0.05, limiter="Superbee",
+                               boundaries=["Reflective"] * 3)
+    cases["s3d_open_albada"] = S(p3, [1.0, 0.9, 0.8], t_end=0.02, limiter="Albada",
+                                 boundaries=["Open", "Periodic", "Reflective"])
+    p1 = np.empty((3, 64))
+    p1[:, :32] = np.array([1.0, 0.0, 1.0])[:, None]
+    p1[:, 32:] = np.array([0.125, 0.0, 0.1])[:, None]
+    cases["s1d_sod"] = S(p1, [1.0], t_end=0.1, limiter="VanLeer")
+    cases["s1d_sod_superbee_reflective"] = S(p1, [1.0], t_end=0.05, limiter="Superbee",
+                                             boundaries=["Reflective"])
+    # reactive 3D (SI kinetics): ignition preset on a tiny grid
+    pi = R.torchSolver3D.get_3d_preset("3d_ignition", 6, 5, 4)["primitive"]
+    cases["s3d_ignition_znd"] = S(pi, [1, 1, 1], t_end=2e-6, reactive=True,
+                                  kinetic_model="znd", limiter="VanLeer")
+    cases["s3d_ignition_arr"] = S(pi, [1, 1, 1], t_end=2e-6, reactive=True,
+                                  kinetic_model="arrhenius", limiter="MINBEE",
+                                  boundaries=["Reflective", "Open", "Periodic"])
+    p2 = np.ones((4, 10, 12))
+    p2[1:3] = 0.0
+    p2[3] = np.where(np.arange(12) < 6, 3e6, 101325.0)[None, :]
+    cases["s2d_reactive"] = S(p2, [1, 1], t_end=1e-6, reactive=True, limiter="Superbee",
+                              boundaries=["Periodic", "Inflow"],
+                              inlet_primitive=[1.0, 0.0, 100.0, 101325.0])
+    p1r = np.empty((3, 40))
+    p1r[:, :20] = np.array([1.0, 0.0, 5e6])[:, None]
+    p1r[:, 20:] = np.array([0.5, 0.0, 101325.0])[:, None]
+    cases["s1d_reactive_znd"] = S(p1r, [1.0], t_end=2e-6, reactive=True,
+                                  kinetic_model="znd")
+    for name, s in cases.items():
+        out[f"{name}_state0"] = s.state.copy()
+        if s.lam is not None:
+            out[f"{name}_lam0"] = s.lam.copy()
+        if s.beta is not None:
+            out[f"{name}_beta0"] = s.beta.copy()
+        for _ in range(8):
+            if s.completed:
+                break
+            s.step()
+        out[f"{name}_state"] = s.state
+        if s.lam is not None:
+            out[f"{name}_lam"] = s.lam
+        if s.beta is not None:
+            out[f"{name}_beta"] = s.beta
+        out[f"{name}_scalars"] = np.array([s.time, s.steps])
+        out[f"{name}_boundary"] = s.boundary_integral
+        out[f"{name}_source"] = s.source_integral
+        out[f"{name}_initial"] = s.initial_integral
+    np.savez_compressed(OUT / "sessions.npz", **out)
+
+
+def large_cfl_case(R):
+    """2D explosion at CFL 0.8 (rejected by Simulation): dt from the session
+    formula, step function called directly, 12 steps on a 40x40 grid."""
+    two = R.torchSolver2D
+    n = 40
+    x = (np.arange(n) + 0.5) * 2.0 / n
+    X, Y = np.meshgrid(x, x)
+    inside = np.hypot(X - 1, Y - 1) <= 0.4
+    prim = np.stack((np.where(inside, 1.0, 0.125), 0 * X, 0 * X, np.where(inside, 1.0, 0.1)))
+    state = prim.copy()
+    state[1:-1] *= prim[0]
+    state[-1] = prim[-1] / 0.4 + 0.5 * prim[0] * np.sum(prim[1:-1] ** 2, axis=0)
+    h = (2.0 / n, 2.0 / n)
+    out = dict(state0=state.copy())
+    dts = []
+    for _ in range(12):
+        padded = two.apply_boundary_conditions_2d(state, "Open", "Open")
+        gp = two.pad_scalar_2d(np.broadcast_to(1.4, state.shape[1:]), "Open", "Open", 1.4)
+        dt = two.compute_cfl_dt_2d(two.uconsv_to_uprim_2d(padded, gp), *h, 0.8, gp)
+        state = two.muscl_hancock_step_2d(state, *h, dt, 1.4, "VanLeer", "Open", "Open")
+        dts.append(dt)
+    out.update(state=state, dts=np.array(dts))
+    np.savez_compressed(OUT / "cfl08_2d.npz", **out)
+
+
+def main():
+    R = load_reference()
+    rng = np.random.default_rng(20261203)
+    hllc_cases(R, rng)
+    step3d_cases(R, rng)
+    step2d_cases(R, rng)
+    chemistry_cases(R, rng)
+    session_cases(R, rng)
+    large_cfl_case(R)
+    for f in sorted(OUT.glob("*.npz")):
+        print(f.name, f.stat().st_size)
+
+
+if __name__ == "__main__":
+    main()
