@@ -1,0 +1,323 @@
+"""Benchmark of the GB300 finite-volume step (one JSON line on stdout).
+
+Workload (default): 3D spherical explosion, 256^3 cells on [0,1]^3, gamma 1.4,
+Superbee limiter, reflective walls, CFL 0.6 — FP32 bulk step with FP64 time and
+conservation sums.  A "step" is one complete session step (fused
+MUSCL-Hancock/HLLC kernel, conditional first-order fallback, finalize with the
+next CFL dt) over the whole grid.  The state (5 x 256^3 x 4 B = 335 MB) is
+larger than L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With --gpus N > 1 (torchrun) every rank advances its own grid ("replicas
+only": the step has no cross-rank exchange); value = total cell updates of
+all ranks / max rank time.  --impl reference times the reference algorithm's
+CPU implementation (the NumPy restatement in oracle/, threaded HLLC batches
+like the reference's Execution pool) on a bounded slab of the same workload.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s FP32 vs FP64 plain @L1<1e-5; batched/served p50/p99 latency"
+UNIT = "cell-updates/s"
+N = 256
+BYTES_PER_CELL = {"fp32": 40, "fp64": 80}  # read + write of 5 conserved values
+
+
+def explosion_3d(n, nz=None):
+    nz = nz or n
+    c = (np.arange(n) + 0.5) / n
+    z = (np.arange(nz) + 0.5) / n + (0.5 - nz / (2 * n))
+    Z, Y, X = np.meshgrid(z, c, c, indexing="ij")
+    inside = (X - 0.5) ** 2 + (Y - 0.5) ** 2 + (Z - 0.5) ** 2 <= 0.2 ** 2
+    p = np.zeros((5, nz, n, n))
+    p[0] = np.where(inside, 1.0, 0.125)
+    p[4] = np.where(inside, 1.0, 0.1)
+    return p
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[4:8]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference(steps, warmup, nz=16, workers=1):
+    """The reference algorithm on the host: NumPy restatement, central z-slab
+    (256 x 256 x nz) of the explosion with reflective walls."""
+    from oracle import fv
+
+    fv.set_workers(workers)
+    prim = explosion_3d(N, nz)
+    state = fv.prim_to_cons(prim, 1.4)
+    h = (1.0 / N,) * 3
+    bcs = ["Reflective"] * 3
+
+    def one(s):
+        dt = fv.dt_3d(s, h, 0.6, 1.4)
+        return fv.hydro_3d(s, 1.4, h, dt, "Superbee", bcs)[0]
+
+    for _ in range(warmup):
+        state = one(state)
+    samples = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        state = one(state)
+        samples.append(time.perf_counter() - t0)
+    cells = N * N * nz
+    return cells / statistics.median(samples), f"{N}x{N}x{nz} central z-slab, median of {steps} steps"
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cores = len(os.sched_getaffinity(0))
+    steps = max(1, min(args.steps, 5))
+    value, sample = cpu_reference(steps, min(args.warmup, 1), workers=cores)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": N ** 3 / value * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "3D spherical explosion 256^3, Superbee, reflective, CFL 0.6",
+                   "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N)
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import torch_gb300
+
+    n = args.n
+    prim = explosion_3d(n)
+    kw = dict(t_end=1e9, cfl=0.6, limiter="Superbee", boundaries=["Reflective"] * 3,
+              strict_cfl=False, max_steps=10 ** 9)
+    sim = torch_gb300.Simulation(prim, [1, 1, 1], precision="fp32", graph_steps=1, **kw)
+    eng = sim._engine
+    stream = eng.stream
+    cells = n ** 3
+    for _ in range(args.warmup):
+        sim.advance(1)
+    sim.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # headline: device-resident throughput
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        barrier()
+        start.record(stream)
+        sim.advance(args.steps)
+        stop.record(stream)
+        barrier()
+    ms = start.elapsed_time(stop) / args.steps
+    steps_done = sim.steps
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * cells / (ms * 1e-3)
+    # per-kernel times of the same step (events around each launch)
+    k = max(3, min(args.steps, 10))
+    t_step, t_fb, t_fin = eng.profile(k)
+    step_kernel_ms = t_step / k
+    hbm, peak_kind = peaks()
+    achieved = BYTES_PER_CELL["fp32"] * cells / (step_kernel_ms * 1e-3) / 1e9
+
+    # end to end: host state in pinned memory, H2D + step + D2H every step
+    cur = eng.current()
+    host_in = torch.empty(cur.shape, dtype=cur.dtype, pin_memory=True)
+    host_out = torch.empty_like(host_in, pin_memory=True)
+    host_in.copy_(cur)
+    torch.cuda.synchronize()
+    e2e_steps = max(3, min(args.steps, 10))
+    s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    s2.record(stream)
+    c = eng.reports[0].current  # ring index of the current state; each step flips it
+    with torch.cuda.stream(stream):
+        for _ in range(e2e_steps):
+            eng.rings[0][c].copy_(host_in, non_blocking=True)
+            eng.replan_async()
+            sim.advance(1)
+            c = (c + 1) % eng.nring
+            host_out.copy_(eng.rings[0][c], non_blocking=True)
+    e2.record(stream)
+    barrier()
+    e2e_ms = s2.elapsed_time(e2) / e2e_steps
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    nbytes = cur.numel() * cur.element_size()
+
+    # FP64 plain path on the same workload (a few steps) and the FP32 error
+    extra = {}
+    if rank == 0:
+        s64 = torch_gb300.Simulation(prim, [1, 1, 1], precision="fp64", **kw)
+        s32 = torch_gb300.Simulation(prim, [1, 1, 1], precision="fp32", **kw)
+        k64 = 10
+        s64.advance(2)
+        s64.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(s64._engine.stream)
+        s64.advance(k64)
+        ev1.record(s64._engine.stream)
+        s64.synchronize()
+        ms64 = ev0.elapsed_time(ev1) / k64
+        s32.advance(2 + k64)
+        s32.synchronize()
+        r64 = s64.device_state[0].double()
+        r32 = s32.device_state[0].double()
+        p64 = s64.device_state
+        extra = {
+            "fp64_plain": {"value": cells / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64},
+            "fp32_over_fp64": (cells / (ms * 1e-3)) / (cells / (ms64 * 1e-3)),
+            "fp32_vs_fp64_after_steps": 2 + k64,
+            "l1_rho": float((r32 - r64).abs().mean()),
+            "linf_rho": float((r32 - r64).abs().max()),
+            "fp32_balance_rel": float(np.max(np.abs(s32.balance_residual))
+                                      / np.max(np.abs(s32.initial_integral))),
+        }
+        del p64
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        v, sample = cpu_reference(3, 1, workers=1)
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "3D spherical explosion 256^3 FP32, Superbee, reflective, "
+                                   "CFL 0.6", "grid": [n, n, n], "precision": "fp32 bulk, fp64 "
+                                   "time and sums", "l2": "state 335 MB > L2, no flush",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "hydro_kernel<float,3>", "kernel_ms": step_kernel_ms,
+                         "bytes_per_cell": BYTES_PER_CELL["fp32"]},
+            "cpu_baseline": cpu,
+            "e2e": {"value": world * cells / (e2e_ms * 1e-3), "unit": UNIT,
+                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                    "ms_per_step": e2e_ms},
+            "gpu_launches": 3 * args.steps,
+            "clocks": clocks.summary(),
+            "steps_completed": steps_done,
+            "fallback_steps": sim.fallback_steps,
+        }
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,211 @@
+/*
+ * tfv.h — C ABI of the GB300 structured-grid finite-volume library
+ * (libtfv.so, built from torch_gb300/csrc).
+ *
+ * The library advances Cartesian 1D/2D/3D Euler / reactive Euler grids with
+ * TORCH's MUSCL-Hancock + HLLC scheme on one GPU.  It replaces the CPU flux
+ * workers behind TORCH's session step:
+ *   python/cfdSolver/torchSession.py:374-522      Simulation.step
+ *   python/cfdSolver/torchExecution.py:17-68      Execution.map (CPU workers)
+ *   python/cfdSolver/torchFlux.py:6-77,125-248    hllc_flux_grid / hllc_flux
+ *   python/cfdSolver/torchSolver2D.py:274-466     muscl_hancock_step_2d
+ *   python/cfdSolver/torchSolver3D.py:122-203     _hydro
+ *
+ * Conventions
+ *  - Every array pointer is a DEVICE pointer owned by the caller (PyTorch
+ *    tensors in the Python host layer).  The library never allocates or frees
+ *    device memory; the caller provides a workspace of the size the library
+ *    asks for.
+ *  - States are (dim+2, nz, ny, nx), x fastest, components
+ *    rho, rho*u, [rho*v], [rho*w], E — the reference layout
+ *    (python/cfdSolver/torchSession.py:146-150, torchIO.py:5-10).
+ *  - Status codes: TFV_OK, TFV_EINVAL (the reference raises ValueError),
+ *    TFV_ENUMERIC (RuntimeError: stall / nonphysical / max steps / no stable
+ *    reactive step; the session state is unchanged), TFV_ECUDA.
+ *  - A batch handle is single-owner and not thread-safe.  Work is enqueued on
+ *    the stream given at bind time; only the report calls synchronise.
+ */
+#ifndef TFV_H
+#define TFV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  TFV_OK = 0,
+  TFV_EINVAL = 1,
+  TFV_ENUMERIC = 2,
+  TFV_ECUDA = 3
+};
+
+enum { TFV_FP64 = 0, TFV_FP32 = 1 };
+
+/* boundary kinds (python/cfdSolver/torchSession.py:237-241) */
+enum { TFV_BC_OPEN = 0, TFV_BC_REFLECTIVE = 1, TFV_BC_PERIODIC = 2, TFV_BC_INFLOW = 3 };
+
+/* limiters (python/cfdSolver/torchSolver3D.py:24) */
+enum { TFV_VANLEER = 0, TFV_ALBADA = 1, TFV_MINBEE = 2, TFV_SUPERBEE = 3, TFV_UNOS = 4 };
+
+enum { TFV_ARRHENIUS = 0, TFV_ZND = 1 };
+/* chemistry closure: TORCH's SI H2/O2 closure (gamma(lambda), T = p M/(rho R))
+ * or the nondimensional one (constant gamma, T = p/rho) */
+enum { TFV_CLOSURE_SI = 0, TFV_CLOSURE_NONDIM = 1 };
+
+/* 1D options (python/cfdSolver/torchSolver.py:1108-1118) */
+enum { TFV_W_SOUND_SPEED = 0, TFV_W_ZERO = 1 };
+enum { TFV_HLLC_VARIANT1 = 0, TFV_HLLC_VARIANT2 = 1 };
+enum { TFV_WAVES_PRESSURE = 0, TFV_WAVES_ENTHALPY = 1 };
+
+/* instance status (tfv_report.status) */
+enum {
+  TFV_READY = 0,          /* next step can run */
+  TFV_DONE = 1,           /* time == t_end: further steps are no-ops */
+  TFV_ERR_MAXSTEPS = 2,   /* steps >= max_steps before t_end */
+  TFV_ERR_STALL = 3,      /* dt not finite, <= 0, or time + dt == time */
+  TFV_ERR_NONPHYSICAL = 4,/* nonphysical even after the first-order fallback */
+  TFV_ERR_REACTIVE = 5,   /* no CFL-stable reactive step in 60 halvings */
+  TFV_ERR_SPECIES = 6,    /* 3D species transport left [-1e-10, 1+1e-10] */
+  TFV_ERR_CHEMISTRY = 7,  /* reaction input invalid (reference ValueError) */
+  TFV_RETRY = 8           /* reactive dt must be halved (host completes the step) */
+};
+
+/* Mirrors Simulation.config for one Cartesian grid
+ * (python/cfdSolver/torchSession.py:66-92). */
+typedef struct tfv_config {
+  int32_t dim;               /* 1, 2 or 3 */
+  int32_t counts[3];         /* cells along x, y, z (unused axes = 1) */
+  double lengths[3];         /* domain lengths along x, y, z */
+  int32_t bc[3];             /* TFV_BC_* per axis x, y, z */
+  int32_t limiter;           /* TFV_VANLEER ... */
+  double gamma;              /* ratio of specific heats (non-reactive / nondim) */
+  double cfl;
+  double t_end;
+  int64_t max_steps;
+  int32_t reactive;          /* 0/1 */
+  int32_t kinetic_model;     /* TFV_ARRHENIUS / TFV_ZND */
+  int32_t closure;           /* TFV_CLOSURE_SI / TFV_CLOSURE_NONDIM */
+  double q_heat;             /* heat release per unit mass and unit lambda */
+  double activation;         /* SI: Ea [J/mol]; nondim: Ea/R */
+  double pre_exponential;
+  double inlet_primitive[4]; /* 2D y-Inflow: rho, u, v, p */
+  int32_t controller;        /* 1D only */
+  int32_t variant;           /* 1D only */
+  int32_t wavespeed;         /* 1D only */
+  double spacing[3];         /* cell sizes; 0 means lengths[k] / counts[k] */
+} tfv_config;
+
+/* Tile shape of the fused step kernel (chosen by the autotuner). */
+typedef struct tfv_tile {
+  int32_t tx;      /* cells along x per tile (threads along x) */
+  int32_t ty;      /* cells along y per tile (3D only; 1 otherwise) */
+  int32_t chunk;   /* planes marched per tile (z in 3D, y in 2D) */
+  int32_t persistent_ctas; /* 0 = one CTA per tile, else grid size of a persistent launch */
+} tfv_tile;
+
+/* Per-instance scalars read back after steps. */
+typedef struct tfv_report {
+  double time;
+  double dt;                 /* dt of the next step (or of the last one if not READY) */
+  double initial_integral[5];
+  double boundary_integral[5];
+  double source_integral[5];
+  int64_t steps;
+  int32_t status;            /* TFV_READY ... */
+  int32_t current;           /* index of the current state buffer in the ring */
+  int32_t fallback_steps;    /* steps that used the first-order fallback */
+  int32_t last_fallback;     /* 1 if the last committed step used it */
+} tfv_report;
+
+typedef struct tfv_batch tfv_batch;
+
+/* Library version string. */
+const char* tfv_version(void);
+
+/* Text of the last error on this thread (static storage). */
+const char* tfv_last_error(void);
+
+/* Create a batch of n instances of one dimension and precision.  Replaces
+ * the construction-time validation of Simulation.__init__
+ * (python/cfdSolver/torchSession.py:24-158, :190-254). */
+int tfv_batch_create(int32_t dim, int32_t precision, int32_t n, const tfv_config* cfgs,
+                     const tfv_tile* tile, tfv_batch** out);
+
+/* Device workspace bytes needed by the batch (tile table, descriptors,
+ * per-tile partials, scalars, 1D scratch). */
+int tfv_batch_workspace_size(const tfv_batch* b, size_t* bytes);
+
+/* Number of state buffers each instance needs in its ring (2, or 3 when
+ * reactive). */
+int tfv_batch_ring_size(const tfv_batch* b, int32_t* nring);
+
+/* Bind device memory.  states[i*nring + k] is ring buffer k of instance i
+ * (each (dim+2)*cells elements of the batch precision); lams / betas likewise
+ * (cells elements each, NULL when unused).  Buffer 0 of each ring holds the
+ * initial state.  Computes the initial integrals and the first dt
+ * (python/cfdSolver/torchSession.py:153-157, :392-396). */
+int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* const* lams,
+                   void* const* betas, void* stream);
+
+/* Enqueue up to nsteps complete split steps for every READY instance
+ * (python/cfdSolver/torchSession.py:374-522).  Instances that finish or fail
+ * stop in place; the others continue.  Asynchronous. */
+int tfv_batch_advance(tfv_batch* b, int32_t nsteps);
+
+/* Capture `steps_per_graph` steps into a CUDA graph and use it for
+ * subsequent tfv_batch_advance calls (0 disables graphs). */
+int tfv_batch_use_graph(tfv_batch* b, int32_t steps_per_graph);
+
+/* Synchronise and copy every instance's scalars into out[0..n).  Completes a
+ * pending reactive dt halving (TFV_RETRY) on the host side before
+ * returning (python/cfdSolver/torchSession.py:401-411). */
+int tfv_batch_report(tfv_batch* b, tfv_report* out);
+
+/* Recompute integrals of the current states into out[n*5] (FP64)
+ * (python/cfdSolver/torchSession.py:285-295). */
+int tfv_batch_integrals(tfv_batch* b, double* out);
+
+/* Re-plan after the caller wrote new values into the current buffers
+ * (recomputes dt and status; keeps time, steps and integrals). */
+int tfv_batch_replan(tfv_batch* b);
+
+/* Optional per-instance face-flux outputs for the next steps (tests and the
+ * reference's return_fluxes=True): flux_x (dim+2, nz, ny, nx+1), flux_y
+ * (dim+2, nz, ny+1, nx), flux_z (dim+2, nz+1, ny, nx), device pointers of the
+ * batch precision, NULL to disable (python/cfdSolver/torchSolver2D.py:466). */
+int tfv_batch_set_flux_outputs(tfv_batch* b, int32_t inst, void* fx, void* fy, void* fz);
+
+/* Run `nsteps` steps with CUDA events around each kernel on the bound stream
+ * and return the summed milliseconds of the fused step kernel, of the
+ * fallback kernel and of the finalize kernel (measurement support for the
+ * roofline figures; results are the same as tfv_batch_advance). */
+int tfv_batch_profile(tfv_batch* b, int32_t nsteps, float* ms_step, float* ms_fallback,
+                      float* ms_finalize);
+
+int tfv_batch_destroy(tfv_batch* b);
+
+/* Stateless HLLC on n faces in the normal basis (rows rho, m_n, m_t...,
+ * E; nv = 4 or 5), per-face gamma_l / gamma_r; fp64 or fp32
+ * (python/cfdSolver/torchFlux.py:125-248). */
+int tfv_hllc_flux(int32_t precision, int32_t nv, int64_t n, const void* ul, const void* ur,
+                  const void* gl, const void* gr, void* out, void* stream);
+
+/* One hydrodynamic step without session bookkeeping, for the reference's
+ * step functions (python/cfdSolver/torchSolver2D.py:274-466,
+ * torchSolver3D.py:122-203): state_in -> state_out with the given dt and
+ * per-cell gamma (NULL: cfg->gamma).  Writes face fluxes when fx/fy/fz are
+ * non-NULL and *used_fallback.  Synchronous; needs a workspace of
+ * tfv_step_workspace_size bytes. */
+int tfv_step_workspace_size(const tfv_config* cfg, int32_t precision, size_t* bytes);
+int tfv_hydro_step(const tfv_config* cfg, int32_t precision, const void* state_in,
+                   void* state_out, const void* gamma_cells, double dt, void* fx, void* fy,
+                   void* fz, void* workspace, int32_t* used_fallback, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TFV_H */

@@ -329,7 +329,25 @@ def hllc(ul, ur, gamma_l=1.4, gamma_r=None):
     return flux
 
 
-def hllc_grid(left, right, gamma_l, gamma_r=None, direction=0):
+_POOL = None
+_WORKERS = 1
+
+
+def set_workers(workers):
+    """Evaluate HLLC in ordered 8192-face batches on a thread pool of this size,
+    as the reference's Execution.map does (torchExecution.py:17-58,
+    torchFlux.py:57-75).  Values are identical for every worker count."""
+    global _POOL, _WORKERS
+    from concurrent.futures import ThreadPoolExecutor
+    if _POOL is not None:
+        _POOL.shutdown(wait=True)
+        _POOL = None
+    _WORKERS = int(workers)
+    if _WORKERS > 1:
+        _POOL = ThreadPoolExecutor(max_workers=_WORKERS, thread_name_prefix="oracle-flux")
+
+
+def hllc_grid(left, right, gamma_l, gamma_r=None, direction=0, batch=8192):
     """Rotate Cartesian components into the normal basis, evaluate HLLC and
     rotate back (torchFlux.py:6-77; batching does not change values)."""
     nv = left.shape[0]
@@ -337,8 +355,22 @@ def hllc_grid(left, right, gamma_l, gamma_r=None, direction=0):
     order = [0, normal] + [m for m in range(1, nv - 1) if m != normal] + [nv - 1]
     gl = np.broadcast_to(gamma_l, left.shape[1:])
     gr = gl if gamma_r is None else np.broadcast_to(gamma_r, left.shape[1:])
-    value = hllc(left[order].reshape(nv, -1), right[order].reshape(nv, -1),
-                 gl.ravel(), gr.ravel())
+    ul = left[order].reshape(nv, -1)
+    ur = right[order].reshape(nv, -1)
+    gl, gr = gl.ravel(), gr.ravel()
+    n = ul.shape[1]
+    if _POOL is None or n <= batch:
+        value = hllc(ul, ur, gl, gr)
+    else:
+        value = np.empty((nv, n))
+        spans = [(a, min(a + batch, n)) for a in range(0, n, batch)]
+
+        def work(span):
+            a, b = span
+            return a, b, hllc(ul[:, a:b], ur[:, a:b], gl[a:b], gr[a:b])
+
+        for a, b, v in _POOL.map(work, spans):
+            value[:, a:b] = v
     out = np.empty(left.shape)
     out[order] = value.reshape((nv,) + left.shape[1:])
     return out

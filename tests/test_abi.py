@@ -1,0 +1,64 @@
+"""C-ABI checks that need no GPU: the library builds, loads and exports every
+function include/tfv.h declares, and the ctypes structs match the C layout."""
+
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from torch_gb300 import _lib
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "tfv.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(tfv_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    names = declared_functions()
+    assert len(names) >= 15
+    for name in names:
+        assert hasattr(lib, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_lib.library_path())],
+                         capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (tfv_[a-z0-9_]+)", out))
+    assert set(names) <= exported
+    assert lib.tfv_version().decode().startswith("tfv")
+
+
+def test_struct_layouts_match_c(tmp_path):
+    src = tmp_path / "sizes.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "tfv.h"\n'
+        "int main(void){printf(\"%zu %zu %zu %zu %zu\\n\", sizeof(tfv_config),"
+        " sizeof(tfv_tile), sizeof(tfv_report), offsetof(tfv_config, spacing),"
+        " offsetof(tfv_report, steps));return 0;}\n")
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    assert got == [C.sizeof(_lib.Config), C.sizeof(_lib.Tile), C.sizeof(_lib.Report),
+                   _lib.Config.spacing.offset, _lib.Report.steps.offset]
+
+
+def test_invalid_arguments_are_rejected_without_a_gpu():
+    lib = _lib.load()
+    handle = C.c_void_p()
+    cfg = _lib.Config()
+    cfg.dim = 3
+    for k in range(3):
+        cfg.counts[k] = 1  # fewer than two cells
+        cfg.lengths[k] = 1.0
+    cfg.gamma, cfg.cfl, cfg.t_end, cfg.max_steps = 1.4, 0.4, 1.0, 10
+    code = lib.tfv_batch_create(3, 0, 1, C.byref(cfg), None, C.byref(handle))
+    assert code == _lib.TFV_EINVAL
+    assert "cells" in _lib.last_error()
+    with pytest.raises(ValueError):
+        _lib.check(code)

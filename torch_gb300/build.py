@@ -1,0 +1,82 @@
+"""Build libtfv.so (the C-ABI CUDA library) in-tree for sm_103a.
+
+    python -m torch_gb300.build
+
+Each translation unit is compiled by nvcc in parallel; the double-precision
+kernels are built with -fmad=false so that they keep NumPy's rounding, the
+single-precision kernels with FMA contraction, flush-to-zero and fast
+division/square root.  Output: torch_gb300/_build/libtfv.so.
+"""
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+INCLUDE = PKG.parent / "include"
+BUILD = PKG / "_build"
+LIB = BUILD / "libtfv.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + str(INCLUDE),
+          "-I" + str(CSRC)]
+UNITS = {
+    "tfv_f64.cu": ["-fmad=false"],
+    "tfv_f32.cu": ["-fmad=true", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
+    "tfv_host.cu": [],
+}
+
+
+def nvcc_path():
+    nvcc = shutil.which("nvcc")
+    if nvcc is None:
+        cand = Path("/usr/local/cuda/bin/nvcc")
+        if cand.exists():
+            return str(cand)
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libtfv")
+    return nvcc
+
+
+def _sources_newer(target):
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    deps = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h")) + [Path(__file__)]
+    return any(p.stat().st_mtime > t for p in deps)
+
+
+def build(force=False, verbose=False):
+    """Compile every unit and link libtfv.so; returns its path."""
+    if not force and not _sources_newer(LIB):
+        return LIB
+    BUILD.mkdir(parents=True, exist_ok=True)
+    nvcc = nvcc_path()
+
+    def compile_unit(item):
+        src, flags = item
+        obj = BUILD / (Path(src).stem + ".o")
+        cmd = [nvcc, *ARCH, *COMMON, *flags, "-c", str(CSRC / src), "-o", str(obj)]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {src}:\n{res.stdout}\n{res.stderr}")
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as pool:
+        objs = list(pool.map(compile_unit, UNITS.items()))
+    tmp = BUILD / "libtfv.so.tmp"
+    cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart_static"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

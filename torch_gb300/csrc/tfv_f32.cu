@@ -1,0 +1,8 @@
+// Single-precision step kernels: the bulk FP32 path (contraction and fast
+// division/square root allowed by the build flags; conservation sums and time
+// stay in double).
+#define REAL float
+#define TFV_LAUNCH_NAME launch_step_f32
+#define TFV_SMEM_NAME hydro_smem_f32
+#define TFV_HLLC_NAME launch_hllc_f32
+#include "tfv_inst.inc"

@@ -1,0 +1,16 @@
+// Double-precision step kernels: the reference-faithful path.  Built with
+// -fmad=false so every product and sum rounds separately, as in NumPy.
+#define REAL double
+#define TFV_DEFINE_SHARED_KERNELS
+#define TFV_LAUNCH_NAME launch_step_f64
+#define TFV_SMEM_NAME hydro_smem_f64
+#define TFV_HLLC_NAME launch_hllc_f64
+#include "tfv_inst.inc"
+
+namespace tfv {
+cudaError_t launch_finalize(const StepArgs& A, int mode, int fp32, double* integrals_out,
+                            cudaStream_t s) {
+  finalize_kernel<<<A.ninst, 256, 0, s>>>(A, mode, fp32, integrals_out);
+  return cudaGetLastError();
+}
+}  // namespace tfv

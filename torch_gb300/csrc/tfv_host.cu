@@ -1,0 +1,545 @@
+// Host side of the C ABI declared in include/tfv.h: validation, tile tables,
+// workspace layout, step sequencing and CUDA-graph capture.  The library
+// never allocates device memory: the caller passes a workspace and the state
+// buffers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "tfv.h"
+#include "tfv_launch.h"
+#include "tfv_types.h"
+
+using namespace tfv;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg) {
+  g_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  g_error = std::string(where) + ": " + cudaGetErrorString(e);
+  return TFV_ECUDA;
+}
+
+#define TFV_CUDA(call)                                   \
+  do {                                                   \
+    cudaError_t e__ = (call);                            \
+    if (e__ != cudaSuccess) return cuda_fail(e__, #call); \
+  } while (0)
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+struct tfv_batch {
+  int dim = 0, precision = 0, n = 0;
+  std::vector<tfv_config> cfg;
+  tfv_tile tile{};
+  bool varg = false;
+  bool reactive = false;
+  int nring = 2;
+  std::vector<InstDesc> desc;
+  std::vector<Tile> tiles;
+  std::vector<InstState> st;
+  // workspace layout (bytes)
+  size_t off_desc = 0, off_st = 0, off_tiles = 0, off_bsum = 0, off_wmax = 0, off_sum = 0,
+         off_flags = 0, off_int = 0, off_gam = 0, total = 0;
+  size_t gam_bytes = 0;
+  unsigned char* ws = nullptr;
+  cudaStream_t stream = nullptr;
+  StepArgs args{};
+  int block = 0, grid = 0;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  bool bound = false;
+};
+
+namespace {
+
+bool valid_bc(int bc, int dim, int axis) {
+  if (bc == TFV_BC_OPEN || bc == TFV_BC_REFLECTIVE || bc == TFV_BC_PERIODIC) return true;
+  return bc == TFV_BC_INFLOW && dim == 2 && axis == 1;
+}
+
+// Construction-time checks of Simulation (python/cfdSolver/torchSession.py:
+// 190-254; validate_grid, torchSolver.py:1074-1088, without its CFL <= 0.5
+// bound, which the Python layer enforces unless told otherwise).
+int validate(const tfv_config& c, int dim) {
+  if (c.dim != dim) return fail(TFV_EINVAL, "instance dimension differs from the batch");
+  for (int k = 0; k < dim; ++k) {
+    if (c.counts[k] < 2) return fail(TFV_EINVAL, "Require cells >= 2 along every axis");
+    if (!(std::isfinite(c.lengths[k]) && c.lengths[k] > 0))
+      return fail(TFV_EINVAL, "Require length > 0");
+    if (!valid_bc(c.bc[k], dim, k)) return fail(TFV_EINVAL, "Unsupported session boundary");
+  }
+  if (!(std::isfinite(c.cfl) && c.cfl > 0)) return fail(TFV_EINVAL, "Require CFL > 0");
+  if (!(std::isfinite(c.t_end) && c.t_end >= 0)) return fail(TFV_EINVAL, "Require t_end >= 0");
+  if (!(std::isfinite(c.gamma) && c.gamma > 1))
+    return fail(TFV_EINVAL, "gamma must be finite and greater than one");
+  if (c.limiter < 0 || c.limiter > 4) return fail(TFV_EINVAL, "Unknown limiter");
+  if (c.max_steps < 1) return fail(TFV_EINVAL, "Invalid maximum steps");
+  if (c.reactive && dim != 1 && false) return fail(TFV_EINVAL, "reactive");
+  return TFV_OK;
+}
+
+void build_tiles(tfv_batch* b) {
+  b->tiles.clear();
+  const int tx = b->tile.tx, ty = b->dim == 3 ? b->tile.ty : 1, ch = b->tile.chunk;
+  for (int i = 0; i < b->n; ++i) {
+    const tfv_config& c = b->cfg[i];
+    InstDesc& d = b->desc[i];
+    d.tile0 = (int)b->tiles.size();
+    const int na = c.counts[0];
+    const int nb = b->dim == 3 ? c.counts[1] : 1;
+    const int np = b->dim == 3 ? c.counts[2] : (b->dim == 2 ? c.counts[1] : 1);
+    for (int p = 0; p < np; p += ch)
+      for (int y = 0; y < nb; y += ty)
+        for (int x = 0; x < na; x += tx) {
+          Tile t{};
+          t.inst = i;
+          t.x0 = x;
+          t.y0 = y;
+          t.p0 = p;
+          t.p1 = std::min(np, p + ch);
+          b->tiles.push_back(t);
+        }
+    d.ntiles = (int)b->tiles.size() - d.tile0;
+  }
+}
+
+void fill_desc(tfv_batch* b, int i) {
+  const tfv_config& c = b->cfg[i];
+  InstDesc& d = b->desc[i];
+  std::memset(&d, 0, sizeof(d));
+  d.dim = b->dim;
+  d.nring = b->nring;
+  double vol = 1.0;
+  d.ncell = 1;
+  for (int k = 0; k < 3; ++k) {
+    d.n[k] = k < b->dim ? c.counts[k] : 1;
+    d.bc[k] = k < b->dim ? c.bc[k] : TFV_BC_OPEN;
+    d.h[k] = k < b->dim ? (c.spacing[k] > 0 ? c.spacing[k] : c.lengths[k] / c.counts[k]) : 1.0;
+    if (k < b->dim) {
+      vol *= d.h[k];
+      d.ncell *= c.counts[k];
+    }
+  }
+  d.vol = vol;
+  d.limiter = c.limiter;
+  d.reactive = c.reactive;
+  d.model = c.kinetic_model;
+  d.closure = c.closure;
+  d.var_gamma = b->varg;
+  d.controller = c.controller;
+  d.variant = c.variant;
+  d.wavespeed = c.wavespeed;
+  d.max_steps = c.max_steps;
+  d.cfl = c.cfl;
+  d.gamma = c.gamma;
+  d.t_end = c.t_end;
+  d.q = c.q_heat;
+  d.ea = c.activation;
+  d.a = c.pre_exponential;
+  // conservative 2D inlet with gamma = 1.4 (python/cfdSolver/torchSolver2D.py:227-243)
+  const double rho = std::max(c.inlet_primitive[0], 1e-12);
+  const double u = c.inlet_primitive[1], v = c.inlet_primitive[2];
+  const double p = std::max(c.inlet_primitive[3], 1e-12);
+  d.inlet[0] = rho;
+  d.inlet[1] = rho * u;
+  d.inlet[2] = rho * v;
+  d.inlet[3] = p / (1.4 - 1.0) + (0.5 * rho) * (u * u + v * v);
+}
+
+size_t real_size(int precision) { return precision == TFV_FP64 ? 8 : 4; }
+
+void layout(tfv_batch* b) {
+  size_t o = 0;
+  const size_t nt = b->tiles.size();
+  b->off_desc = o;
+  o = align_up(o + sizeof(InstDesc) * b->n, 256);
+  b->off_st = o;
+  o = align_up(o + sizeof(InstState) * b->n, 256);
+  b->off_tiles = o;
+  o = align_up(o + sizeof(Tile) * nt, 256);
+  b->off_bsum = o;
+  o = align_up(o + sizeof(double) * 15 * nt, 256);
+  b->off_wmax = o;
+  o = align_up(o + sizeof(double) * 3 * nt, 256);
+  b->off_sum = o;
+  o = align_up(o + sizeof(double) * 5 * nt, 256);
+  b->off_flags = o;
+  o = align_up(o + sizeof(int32_t) * nt, 256);
+  b->off_int = o;
+  o = align_up(o + sizeof(double) * 5 * b->n, 256);
+  b->off_gam = o;
+  b->gam_bytes = 0;
+  if (b->varg) {
+    for (int i = 0; i < b->n; ++i) b->gam_bytes += align_up(real_size(b->precision) * b->desc[i].ncell, 256);
+  }
+  o += b->gam_bytes;
+  b->total = align_up(o, 256);
+}
+
+cudaError_t launch(tfv_batch* b, int op, int src_off, int dst_off) {
+  StepArgs A = b->args;
+  A.src_off = src_off;
+  A.dst_off = dst_off;
+  if (b->precision == TFV_FP64)
+    return launch_step_f64(op, b->dim, b->varg, A, b->grid, b->block, b->stream);
+  return launch_step_f32(op, b->dim, b->varg, A, b->grid, b->block, b->stream);
+}
+
+cudaError_t finalize(tfv_batch* b, int mode, int dst_off) {
+  StepArgs A = b->args;
+  A.dst_off = dst_off;
+  return launch_finalize(A, mode, b->precision == TFV_FP32,
+                         reinterpret_cast<double*>(b->ws + b->off_int), b->stream);
+}
+
+// Enqueue one complete non-reactive step for every READY instance.
+cudaError_t enqueue_step(tfv_batch* b) {
+  cudaError_t e = launch(b, kOpHydro, 0, 1);
+  if (e != cudaSuccess) return e;
+  e = launch(b, kOpFallback, 0, 1);
+  if (e != cudaSuccess) return e;
+  return finalize(b, 0, 1);
+}
+
+int check_bound(const tfv_batch* b) {
+  if (!b) return fail(TFV_EINVAL, "null batch");
+  if (!b->bound) return fail(TFV_EINVAL, "batch is not bound to memory");
+  return TFV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tfv_version(void) { return "tfv 0.1 (sm_103a)"; }
+
+const char* tfv_last_error(void) { return g_error.c_str(); }
+
+static int create_internal(int32_t dim, int32_t precision, int32_t n, const tfv_config* cfgs,
+                           const tfv_tile* tile, bool varg, tfv_batch** out);
+
+int tfv_batch_create(int32_t dim, int32_t precision, int32_t n, const tfv_config* cfgs,
+                     const tfv_tile* tile, tfv_batch** out) {
+  return create_internal(dim, precision, n, cfgs, tile, false, out);
+}
+
+static int create_internal(int32_t dim, int32_t precision, int32_t n, const tfv_config* cfgs,
+                           const tfv_tile* tile, bool varg, tfv_batch** out) {
+  if (!out || !cfgs || n < 1) return fail(TFV_EINVAL, "invalid arguments");
+  if (dim != 2 && dim != 3) return fail(TFV_EINVAL, "dimension must be 2 or 3 for a batch");
+  if (precision != TFV_FP64 && precision != TFV_FP32) return fail(TFV_EINVAL, "bad precision");
+  for (int i = 0; i < n; ++i) {
+    const int r = validate(cfgs[i], dim);
+    if (r != TFV_OK) return r;
+    if (cfgs[i].reactive) return fail(TFV_EINVAL, "reactive batches are not supported yet");
+  }
+  tfv_batch* b = new tfv_batch();
+  b->dim = dim;
+  b->precision = precision;
+  b->n = n;
+  b->cfg.assign(cfgs, cfgs + n);
+  if (tile) {
+    b->tile = *tile;
+  } else {
+    b->tile.tx = dim == 3 ? 32 : 128;
+    b->tile.ty = dim == 3 ? (precision == TFV_FP64 ? 4 : 8) : 1;
+    b->tile.chunk = dim == 3 ? 64 : 32;
+    b->tile.persistent_ctas = 0;
+  }
+  if (dim != 3) b->tile.ty = 1;
+  if (b->tile.tx < 4 || b->tile.ty < 1 || b->tile.chunk < 1 || b->tile.tx * b->tile.ty > 256) {
+    delete b;
+    return fail(TFV_EINVAL, "tile shape must have tx >= 4, ty >= 1, chunk >= 1, tx*ty <= 256");
+  }
+  b->varg = varg;
+  b->nring = 2;
+  b->desc.resize(n);
+  for (int i = 0; i < n; ++i) fill_desc(b, i);
+  build_tiles(b);
+  layout(b);
+  b->st.assign(n, InstState{});
+  *out = b;
+  return TFV_OK;
+}
+
+int tfv_batch_workspace_size(const tfv_batch* b, size_t* bytes) {
+  if (!b || !bytes) return fail(TFV_EINVAL, "invalid arguments");
+  *bytes = b->total;
+  return TFV_OK;
+}
+
+int tfv_batch_ring_size(const tfv_batch* b, int32_t* nring) {
+  if (!b || !nring) return fail(TFV_EINVAL, "invalid arguments");
+  *nring = b->nring;
+  return TFV_OK;
+}
+
+int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* const* lams,
+                   void* const* betas, void* stream) {
+  if (!b || !workspace || !states) return fail(TFV_EINVAL, "invalid arguments");
+  if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
+    return fail(TFV_EINVAL, "workspace must be 256-byte aligned");
+  b->ws = static_cast<unsigned char*>(workspace);
+  b->stream = static_cast<cudaStream_t>(stream);
+  for (int i = 0; i < b->n; ++i) {
+    InstDesc& d = b->desc[i];
+    for (int k = 0; k < b->nring; ++k) {
+      d.U[k] = states[i * b->nring + k];
+      if (!d.U[k]) return fail(TFV_EINVAL, "null state buffer");
+      d.lam[k] = lams ? lams[i * b->nring + k] : nullptr;
+      d.beta[k] = betas ? betas[i * b->nring + k] : nullptr;
+    }
+    d.has_flux_out = 0;
+  }
+  for (int i = 0; i < b->n; ++i) {
+    InstState& s = b->st[i];
+    std::memset(&s, 0, sizeof(s));
+    s.status = TFV_READY;
+  }
+  StepArgs& A = b->args;
+  A.desc = reinterpret_cast<const InstDesc*>(b->ws + b->off_desc);
+  A.st = reinterpret_cast<InstState*>(b->ws + b->off_st);
+  A.tiles = reinterpret_cast<const Tile*>(b->ws + b->off_tiles);
+  A.ntiles = (int)b->tiles.size();
+  A.tx = b->tile.tx;
+  A.ty = b->tile.ty;
+  A.ninst = b->n;
+  A.t_bsum = reinterpret_cast<double*>(b->ws + b->off_bsum);
+  A.t_wmax = reinterpret_cast<double*>(b->ws + b->off_wmax);
+  A.t_sum = reinterpret_cast<double*>(b->ws + b->off_sum);
+  A.t_flags = reinterpret_cast<int32_t*>(b->ws + b->off_flags);
+  b->block = b->tile.tx * b->tile.ty;
+  b->grid = b->tile.persistent_ctas > 0 ? std::min<int>(b->tile.persistent_ctas, A.ntiles)
+                                        : A.ntiles;
+  TFV_CUDA(cudaMemcpyAsync(b->ws + b->off_desc, b->desc.data(), sizeof(InstDesc) * b->n,
+                           cudaMemcpyHostToDevice, b->stream));
+  TFV_CUDA(cudaMemcpyAsync(b->ws + b->off_st, b->st.data(), sizeof(InstState) * b->n,
+                           cudaMemcpyHostToDevice, b->stream));
+  TFV_CUDA(cudaMemcpyAsync(b->ws + b->off_tiles, b->tiles.data(), sizeof(Tile) * b->tiles.size(),
+                           cudaMemcpyHostToDevice, b->stream));
+  // initial integrals and first dt
+  TFV_CUDA(launch(b, kOpWaves, 0, 0));
+  TFV_CUDA(finalize(b, 3, 0));
+  TFV_CUDA(cudaStreamSynchronize(b->stream));
+  b->bound = true;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  return TFV_OK;
+}
+
+int tfv_batch_use_graph(tfv_batch* b, int32_t steps_per_graph) {
+  int r = check_bound(b);
+  if (r) return r;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  b->graph_steps = 0;
+  if (steps_per_graph <= 0) return TFV_OK;
+  cudaGraph_t g = nullptr;
+  TFV_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < steps_per_graph && e == cudaSuccess; ++k) e = enqueue_step(b);
+  cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+  if (e != cudaSuccess) return cuda_fail(e, "capture");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  b->graph_steps = steps_per_graph;
+  return TFV_OK;
+}
+
+int tfv_batch_advance(tfv_batch* b, int32_t nsteps) {
+  int r = check_bound(b);
+  if (r) return r;
+  int k = 0;
+  if (b->graph && b->graph_steps > 0) {
+    for (; k + b->graph_steps <= nsteps; k += b->graph_steps)
+      TFV_CUDA(cudaGraphLaunch(b->graph, b->stream));
+  }
+  for (; k < nsteps; ++k) TFV_CUDA(enqueue_step(b));
+  return TFV_OK;
+}
+
+int tfv_batch_report(tfv_batch* b, tfv_report* out) {
+  int r = check_bound(b);
+  if (r) return r;
+  TFV_CUDA(cudaMemcpyAsync(b->st.data(), b->ws + b->off_st, sizeof(InstState) * b->n,
+                           cudaMemcpyDeviceToHost, b->stream));
+  TFV_CUDA(cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < b->n; ++i) {
+    const InstState& s = b->st[i];
+    tfv_report& o = out[i];
+    std::memset(&o, 0, sizeof(o));
+    o.time = s.time;
+    o.dt = s.dt;
+    for (int c = 0; c < 5; ++c) {
+      o.initial_integral[c] = s.initial[c];
+      o.boundary_integral[c] = s.boundary[c];
+      o.source_integral[c] = s.source[c];
+    }
+    o.steps = s.steps;
+    o.status = s.status;
+    o.current = s.cur;
+    o.fallback_steps = s.fallback_steps;
+    o.last_fallback = s.last_fallback;
+  }
+  return TFV_OK;
+}
+
+int tfv_batch_integrals(tfv_batch* b, double* out) {
+  int r = check_bound(b);
+  if (r) return r;
+  TFV_CUDA(launch(b, kOpWaves, 0, 0));
+  TFV_CUDA(finalize(b, 2, 0));
+  TFV_CUDA(cudaMemcpyAsync(out, b->ws + b->off_int, sizeof(double) * 5 * b->n,
+                           cudaMemcpyDeviceToHost, b->stream));
+  TFV_CUDA(cudaStreamSynchronize(b->stream));
+  return TFV_OK;
+}
+
+int tfv_batch_replan(tfv_batch* b) {
+  int r = check_bound(b);
+  if (r) return r;
+  TFV_CUDA(launch(b, kOpWaves, 0, 0));
+  TFV_CUDA(finalize(b, 1, 0));
+  return TFV_OK;
+}
+
+int tfv_batch_set_flux_outputs(tfv_batch* b, int32_t inst, void* fx, void* fy, void* fz) {
+  int r = check_bound(b);
+  if (r) return r;
+  if (inst < 0 || inst >= b->n) return fail(TFV_EINVAL, "instance out of range");
+  InstDesc& d = b->desc[inst];
+  d.flux_out[0] = fx;
+  d.flux_out[1] = fy;
+  d.flux_out[2] = fz;
+  d.has_flux_out = (fx || fy || fz) ? 1 : 0;
+  TFV_CUDA(cudaMemcpyAsync(b->ws + b->off_desc + sizeof(InstDesc) * inst, &d, sizeof(InstDesc),
+                           cudaMemcpyHostToDevice, b->stream));
+  TFV_CUDA(cudaStreamSynchronize(b->stream));
+  return TFV_OK;
+}
+
+int tfv_batch_profile(tfv_batch* b, int32_t nsteps, float* ms_step, float* ms_fallback,
+                      float* ms_finalize) {
+  int r = check_bound(b);
+  if (r) return r;
+  cudaEvent_t ev[4];
+  for (auto& e : ev) TFV_CUDA(cudaEventCreate(&e));
+  float acc[3] = {0.f, 0.f, 0.f};
+  for (int k = 0; k < nsteps; ++k) {
+    TFV_CUDA(cudaEventRecord(ev[0], b->stream));
+    TFV_CUDA(launch(b, kOpHydro, 0, 1));
+    TFV_CUDA(cudaEventRecord(ev[1], b->stream));
+    TFV_CUDA(launch(b, kOpFallback, 0, 1));
+    TFV_CUDA(cudaEventRecord(ev[2], b->stream));
+    TFV_CUDA(finalize(b, 0, 1));
+    TFV_CUDA(cudaEventRecord(ev[3], b->stream));
+    TFV_CUDA(cudaEventSynchronize(ev[3]));
+    for (int i = 0; i < 3; ++i) {
+      float ms = 0.f;
+      TFV_CUDA(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+      acc[i] += ms;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (ms_step) *ms_step = acc[0];
+  if (ms_fallback) *ms_fallback = acc[1];
+  if (ms_finalize) *ms_finalize = acc[2];
+  return TFV_OK;
+}
+
+int tfv_batch_destroy(tfv_batch* b) {
+  if (!b) return TFV_OK;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  delete b;
+  return TFV_OK;
+}
+
+int tfv_hllc_flux(int32_t precision, int32_t nv, int64_t n, const void* ul, const void* ur,
+                  const void* gl, const void* gr, void* out, void* stream) {
+  if ((nv != 4 && nv != 5) || n < 0 || !ul || !ur || !gl || !gr || !out)
+    return fail(TFV_EINVAL, "HLLC requires matching (4,m) or (5,m) states");
+  if (n == 0) return TFV_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = precision == TFV_FP64 ? launch_hllc_f64(nv, n, ul, ur, gl, gr, out, s)
+                                        : launch_hllc_f32(nv, n, ul, ur, gl, gr, out, s);
+  if (e != cudaSuccess) return cuda_fail(e, "hllc kernel");
+  return TFV_OK;
+}
+
+static tfv_config single_step_config(const tfv_config* cfg) {
+  tfv_config c = *cfg;
+  c.t_end = 1e300;
+  c.max_steps = INT64_MAX;
+  c.reactive = 0;
+  return c;
+}
+
+int tfv_step_workspace_size(const tfv_config* cfg, int32_t precision, size_t* bytes) {
+  if (!cfg || !bytes) return fail(TFV_EINVAL, "invalid arguments");
+  tfv_config c = single_step_config(cfg);
+  tfv_batch* b = nullptr;
+  const int r = create_internal(cfg->dim, precision, 1, &c, nullptr, true, &b);
+  if (r) return r;
+  *bytes = b->total;
+  tfv_batch_destroy(b);
+  return TFV_OK;
+}
+
+int tfv_hydro_step(const tfv_config* cfg, int32_t precision, const void* state_in,
+                   void* state_out, const void* gamma_cells, double dt, void* fx, void* fy,
+                   void* fz, void* workspace, int32_t* used_fallback, void* stream) {
+  if (!cfg || !state_in || !state_out || !workspace) return fail(TFV_EINVAL, "invalid arguments");
+  if (!(std::isfinite(dt) && dt >= 0)) return fail(TFV_EINVAL, "dt must be finite and >= 0");
+  tfv_config c = single_step_config(cfg);
+  tfv_batch* b = nullptr;
+  int r = create_internal(cfg->dim, precision, 1, &c, nullptr, gamma_cells != nullptr, &b);
+  if (r) return r;
+  b->desc[0].gam = const_cast<void*>(gamma_cells);
+  void* ring[2] = {const_cast<void*>(state_in), state_out};
+  r = tfv_batch_bind(b, workspace, ring, nullptr, nullptr, stream);
+  if (!r) r = tfv_batch_set_flux_outputs(b, 0, fx, fy, fz);
+  if (!r) {
+    // the step uses the caller's dt instead of the planned one
+    InstState s = b->st[0];
+    s.dt = dt;
+    s.status = TFV_READY;
+    cudaError_t e = cudaMemcpyAsync(b->ws + b->off_st, &s, sizeof(s), cudaMemcpyHostToDevice,
+                                    b->stream);
+    if (e == cudaSuccess) e = enqueue_step(b);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&s, b->ws + b->off_st, sizeof(s),
+                                              cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) {
+      r = cuda_fail(e, "tfv_hydro_step");
+    } else {
+      if (used_fallback) *used_fallback = s.last_fallback;
+      if (s.status == TFV_ERR_NONPHYSICAL)
+        r = fail(TFV_ENUMERIC, "Hydrodynamic update produced a nonphysical state");
+    }
+  }
+  tfv_batch_destroy(b);
+  return r;
+}
+
+}  // extern "C"

@@ -1,0 +1,1037 @@
+// Kernels of the batched finite-volume engine (2D / 3D).
+//
+// hydro_kernel — the fused step.  A CTA owns a tile of TX x TY cells in the
+// (x, y) plane of a 3D grid (TX cells along x of a 2D grid) and marches
+// along the last axis (z in 3D, y in 2D) through a chunk of planes.  Per
+// plane it
+//   1. stages the conserved state of plane p+1 with a 2-cell in-plane halo
+//      in shared memory (ghost cells by the boundary rules), keeping planes
+//      p-1, p, p+1 in a 3-slot ring;
+//   2. computes limited slopes and the Hancock predictor on the tile plus a
+//      1-cell in-plane ring (the "cross" region), and stores predictor and
+//      in-plane slopes in shared memory;
+//   3. evaluates HLLC on every in-plane face of the tile once;
+//   4. evaluates HLLC on the marching-axis face below each owned cell from
+//      registers (the face state above the previous plane is carried), and
+//      finishes the conservative update of plane p-1 in registers, in the
+//      reference's order U - cx dFx - cy dFy - cz dFz.
+// Each cell's state is read from HBM once per step (plus the in-plane halo,
+// served by L2) and written once.  The epilogue reduces, per tile, the wave
+// speeds of the new state for the next CFL dt, the boundary-face flux sums
+// for the conservation audit and the positivity flags.
+//
+// Reference: python/cfdSolver/torchSolver3D.py:122-203 (_hydro),
+// python/cfdSolver/torchSolver2D.py:274-466 (muscl_hancock_step_2d),
+// python/cfdSolver/torchFlux.py:6-248, python/cfdSolver/torchSession.py:
+// 333-360 (dt), 498-508 (boundary integral).
+#pragma once
+
+#include "tfv_physics.cuh"
+#include "tfv_types.h"
+
+namespace tfv {
+
+enum : int { kBcOpen = 0, kBcReflective = 1, kBcPeriodic = 2, kBcInflow = 3 };
+enum : int { kReady = 0, kDone = 1, kErrMaxSteps = 2, kErrStall = 3, kErrNonphysical = 4,
+             kErrReactive = 5, kErrSpecies = 6, kErrChemistry = 7, kRetry = 8 };
+
+// Source index of padded coordinate i on an axis of n >= 2 cells (at most two
+// cells outside), following np.pad 'edge' / 'symmetric' / 'wrap'
+// (python/cfdSolver/torchSolver3D.py:47-70).
+__device__ __forceinline__ int map_axis(int i, int n, int bc, bool& ghost) {
+  ghost = (i < 0) || (i >= n);
+  if (!ghost) return i;
+  if (bc == kBcReflective) return i < 0 ? -1 - i : 2 * n - 1 - i;
+  if (bc == kBcPeriodic) return i < 0 ? i + n : i - n;
+  return i < 0 ? 0 : n - 1;
+}
+
+// --------------------------------------------------------------------------
+// Deterministic block reductions (fixed shuffle tree, warps summed in order).
+// --------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ int warp_or(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v |= __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum of `v` over the block; result valid in thread 0.  scratch >= 32 doubles.
+__device__ __forceinline__ double block_sum(double v, double* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) scratch[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < nw; ++w) t += scratch[w];
+  }
+  return t;
+}
+__device__ __forceinline__ double block_max(double v, double* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) scratch[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < nw; ++w) t = fmax(t, scratch[w]);
+  }
+  return t;
+}
+__device__ __forceinline__ int block_or(int v, int* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  v = warp_or(v);
+  __syncthreads();
+  if (lane == 0) scratch[warp] = v;
+  __syncthreads();
+  int t = 0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < nw; ++w) t |= scratch[w];
+  }
+  return t;
+}
+
+// --------------------------------------------------------------------------
+// Geometry helper: the grid seen as planes along the marching axis.
+// 3D: (a, b, p) = (x, y, z); 2D: (a, b, p) = (x, -, y).
+// --------------------------------------------------------------------------
+template <int DIM>
+struct Geo {
+  int na, nb, np;   // extents
+  int bca, bcb, bcp;
+  int64_t ps, cs;   // plane stride, component stride
+  __device__ __forceinline__ void init(const InstDesc& d) {
+    na = d.n[0];
+    nb = DIM == 3 ? d.n[1] : 1;
+    np = d.n[DIM - 1];
+    bca = d.bc[0];
+    bcb = DIM == 3 ? d.bc[1] : kBcOpen;
+    bcp = d.bc[DIM - 1];
+    ps = (int64_t)na * nb;
+    cs = ps * np;
+  }
+};
+
+// Value of component c (c == NV: gamma) at padded coordinates (a, b, p).
+template <typename R, int DIM>
+__device__ __forceinline__ R fetch_padded(const InstDesc& d, const Geo<DIM>& g, const R* U,
+                                          const R* gam, int c, int a, int b, int p) {
+  constexpr int NV = DIM + 2;
+  bool ga, gb = false, gp;
+  const int sa = map_axis(a, g.na, g.bca, ga);
+  const int sb = DIM == 3 ? map_axis(b, g.nb, g.bcb, gb) : 0;
+  const int sp = map_axis(p, g.np, g.bcp, gp);
+  if (DIM == 2 && g.bcp == kBcInflow && p < 0) {
+    return c < NV ? R(d.inlet[c]) : R(1.4);
+  }
+  const int64_t off = (int64_t)sp * g.ps + (int64_t)sb * g.na + sa;
+  if (c == NV) return gam ? gam[off] : R(d.gamma);
+  R v = U[c * g.cs + off];
+  if ((c == 1 && ga && g.bca == kBcReflective) ||
+      (DIM == 3 && c == 2 && gb && g.bcb == kBcReflective) ||
+      (c == DIM && gp && g.bcp == kBcReflective))
+    v = -v;
+  return v;
+}
+
+// --------------------------------------------------------------------------
+// Shared-memory layout of one hydro tile.
+// --------------------------------------------------------------------------
+template <typename R, int DIM, bool VARG>
+struct HydroSmem {
+  static constexpr int NV = DIM + 2;
+  static constexpr int NL = NV + (VARG ? 1 : 0);
+  int tx, ty, pw, ph, bw, bh;
+  size_t ring_off, box_off, fa_off, fb_off, bs_off, red_off, bytes;
+  __host__ __device__ void init(int tx_, int ty_) {
+    tx = tx_;
+    ty = DIM == 3 ? ty_ : 1;
+    pw = tx + 4;
+    ph = DIM == 3 ? ty + 4 : 1;
+    bw = tx + 2;
+    bh = DIM == 3 ? ty + 2 : 1;
+    size_t o = 0;
+    ring_off = o;
+    o += sizeof(R) * 3 * NL * ph * pw;
+    o = (o + 15) & ~size_t(15);
+    box_off = o;
+    o += sizeof(R) * (DIM == 3 ? 3 : 2) * NV * bh * bw;
+    o = (o + 15) & ~size_t(15);
+    fa_off = o;
+    o += sizeof(R) * NV * ty * (tx + 1);
+    o = (o + 15) & ~size_t(15);
+    fb_off = o;
+    if (DIM == 3) o += sizeof(R) * NV * (ty + 1) * tx;
+    o = (o + 15) & ~size_t(15);
+    bs_off = o;  // boundary-face accumulators (double)
+    o += sizeof(double) * (2 * ty * NV + (DIM == 3 ? 2 * tx * NV : 0) + 2 * NV);
+    red_off = o;  // reduction scratch
+    o += sizeof(double) * 40;
+    bytes = (o + 15) & ~size_t(15);
+  }
+};
+
+template <typename R, int DIM, bool VARG>
+struct HydroTile {
+  static constexpr int NV = DIM + 2;
+  static constexpr int NL = NV + (VARG ? 1 : 0);
+  static constexpr int MD = DIM - 1;  // marching direction
+
+  // Stage plane p of the padded state (2-cell in-plane halo) into `dst`.
+  static __device__ __forceinline__ void load_plane(const InstDesc& d, const Geo<DIM>& g,
+                                                    const R* U, const R* gam, R* dst,
+                                                    const HydroSmem<R, DIM, VARG>& S, int x0,
+                                                    int y0, int ax, int by, int p) {
+    const int w = ax + 4;
+    const int h = DIM == 3 ? by + 4 : 1;
+    const int plane = S.ph * S.pw;
+    const bool inside_p = (p >= 0 && p < g.np);
+    const bool inside_a = (x0 >= 2 && x0 + ax + 2 <= g.na);
+    const bool inside_b = DIM == 2 || (y0 >= 2 && y0 + by + 2 <= g.nb);
+    const int n = NL * h * w;
+    if (inside_p && inside_a && inside_b) {
+      const int64_t base = (int64_t)p * g.ps + (int64_t)(DIM == 3 ? y0 - 2 : 0) * g.na + (x0 - 2);
+      for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int c = e / (h * w);
+        const int r = e - c * (h * w);
+        const int lb = r / w;
+        const int la = r - lb * w;
+        const int64_t off = base + (int64_t)lb * g.na + la;
+        R v;
+        if (VARG && c == NV)
+          v = gam[off];
+        else
+          v = U[c * g.cs + off];
+        dst[c * plane + lb * S.pw + la] = v;
+      }
+    } else {
+      for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int c = e / (h * w);
+        const int r = e - c * (h * w);
+        const int lb = r / w;
+        const int la = r - lb * w;
+        dst[c * plane + lb * S.pw + la] = fetch_padded<R, DIM>(
+            d, g, U, VARG ? gam : (const R*)nullptr, c, x0 - 2 + la, DIM == 3 ? y0 - 2 + lb : 0, p);
+      }
+    }
+  }
+};
+
+// Cell stage at local position (a, b) of the current plane: limited slopes in
+// every direction and the Hancock predictor (python/cfdSolver/torchSolver3D.py:
+// 135-151, python/cfdSolver/torchSolver2D.py:305-377).  Writes predictor and
+// in-plane slopes to the box; returns the marching-axis slope; sets *gate when
+// a predicted face state is nonphysical (3D gate, torchSolver3D.py:152-159).
+template <typename R, int DIM, bool VARG>
+__device__ __forceinline__ void cell_stage(const R* ringm, const R* ringc, const R* ringp,
+                                           R* box, const HydroSmem<R, DIM, VARG>& S, int a,
+                                           int b, int limiter, R gconst, const R* coefh,
+                                           R* ubar, R* smarch, bool& gate) {
+  constexpr int NV = DIM + 2;
+  const int plane = S.ph * S.pw;
+  const int li = (DIM == 3 ? (b + 2) * S.pw : 0) + (a + 2);
+  const int bi = (DIM == 3 ? (b + 1) * S.bw : 0) + (a + 1);
+  const int bplane = S.bh * S.bw;
+  R* bub = box;                   // predictor
+  R* bsa = box + NV * bplane;     // slope along a (x)
+  R* bsb = box + 2 * NV * bplane; // slope along b (y), 3D only
+  const R g = VARG ? ringc[NV * plane + li] : gconst;
+
+  R u[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) {
+    u[c] = ringc[c * plane + li];
+    ubar[c] = u[c];
+  }
+#pragma unroll
+  for (int dd = 0; dd < DIM; ++dd) {
+    R s[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+      R um, up;
+      if (dd == 0) {
+        um = ringc[c * plane + li - 1];
+        up = ringc[c * plane + li + 1];
+      } else if (dd == (DIM - 1)) {
+        um = ringm[c * plane + li];
+        up = ringp[c * plane + li];
+      } else {
+        um = ringc[c * plane + li - S.pw];
+        up = ringc[c * plane + li + S.pw];
+      }
+      s[c] = limited_slope<R, DIM>(um, u[c], up, limiter);
+    }
+    R vp[NV], vm[NV], fp[NV], fm[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+      vp[c] = u[c] + R(0.5) * s[c];
+      vm[c] = u[c] - R(0.5) * s[c];
+    }
+    if (DIM == 3) {
+      flux3<R>(vp, g, dd + 1, fp);
+      flux3<R>(vm, g, dd + 1, fm);
+    } else {
+      flux2<R>(vp, g, dd, fp);
+      flux2<R>(vm, g, dd, fm);
+    }
+#pragma unroll
+    for (int c = 0; c < NV; ++c) ubar[c] = ubar[c] - coefh[dd] * (fp[c] - fm[c]);
+    if (dd == 0) {
+#pragma unroll
+      for (int c = 0; c < NV; ++c) bsa[c * bplane + bi] = s[c];
+    } else if (dd == (DIM - 1)) {
+#pragma unroll
+      for (int c = 0; c < NV; ++c) smarch[c] = s[c];
+    } else {
+#pragma unroll
+      for (int c = 0; c < NV; ++c) bsb[c * bplane + bi] = s[c];
+    }
+  }
+  if (DIM == 2) {
+    // predictor floors (python/cfdSolver/torchSolver2D.py:367-377)
+    ubar[0] = np_max(ubar[0], R(kFloor));
+    const R ke = (R(0.5) * (ubar[1] * ubar[1] + ubar[2] * ubar[2])) / ubar[0];
+    const R pb = (g - R(1)) * (ubar[3] - ke);
+    if (pb < R(kFloor)) ubar[3] = R(kFloor) / (g - R(1)) + ke;
+  }
+#pragma unroll
+  for (int c = 0; c < NV; ++c) bub[c * bplane + bi] = ubar[c];
+  if (DIM == 3) {
+    // predictor gate on every predicted face state
+    bool ok = true;
+#pragma unroll
+    for (int dd = 0; dd < DIM; ++dd) {
+      R lo[NV], hi[NV];
+#pragma unroll
+      for (int c = 0; c < NV; ++c) {
+        const R s = dd == 0 ? bsa[c * bplane + bi]
+                            : (dd == 1 ? bsb[c * bplane + bi] : smarch[c]);
+        lo[c] = ubar[c] + R(-0.5) * s;
+        hi[c] = ubar[c] + R(0.5) * s;
+      }
+      ok = ok && physical_cell<R, NV>(lo) && physical_cell<R, NV>(hi);
+    }
+    if (!ok) gate = true;
+  }
+}
+
+// Wave speeds max(|u_d| + a) of one updated cell for the next CFL dt.
+// 3D: session _dt (python/cfdSolver/torchSession.py:356-360, no floors).
+// 2D: compute_cfl_dt_2d on floored primitives (torchSolver2D.py:512-530).
+template <typename R, int DIM>
+__device__ __forceinline__ void wave_speeds(const R* u, R g, R* w) {
+  if (DIM == 3) {
+    const R rho = u[0];
+    const R s = (u[1] * u[1] + u[2] * u[2]) + u[3] * u[3];
+    const R p = (g - R(1)) * (u[4] - (R(0.5) * s) / rho);
+    const R a = sqrt((g * p) / rho);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) w[k] = fabs(u[k + 1] / rho) + a;
+  } else {
+    const R rho = np_max(u[0], R(kFloor));
+    const R vx = u[1] / rho;
+    const R vy = u[2] / rho;
+    const R p = np_max((g - R(1)) * (u[3] - (R(0.5) * rho) * (vx * vx + vy * vy)), R(kFloor));
+    const R a = sqrt((g * np_max(p, R(kFloor))) / np_max(rho, R(kFloor)));
+    w[0] = fabs(vx) + a;
+    w[1] = fabs(vy) + a;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T* smem_at(unsigned char* base, size_t off) {
+  return reinterpret_cast<T*>(base + off);
+}
+
+// One tile of the fused second-order step.
+template <typename R, int DIM, bool VARG>
+__device__ void hydro_tile(const StepArgs& A, int t, unsigned char* smem,
+                           const HydroSmem<R, DIM, VARG>& S) {
+  constexpr int NV = DIM + 2;
+  constexpr int NL = NV + (VARG ? 1 : 0);
+  constexpr int MD = DIM - 1;
+  const Tile T = A.tiles[t];
+  const InstDesc& d = A.desc[T.inst];
+  InstState& st = A.st[T.inst];
+  if (st.status != kReady) return;  // uniform over the CTA
+  Geo<DIM> g;
+  g.init(d);
+  const int src = (st.cur + A.src_off) % d.nring;
+  const int dst = (st.cur + A.dst_off) % d.nring;
+  const R* U = (const R*)d.U[src];
+  R* Un = (R*)d.U[dst];
+  const R* gam = VARG ? (const R*)d.gam : nullptr;
+  const double dt = st.dt;
+  const int limiter = d.limiter;
+  const R gconst = R(d.gamma);
+  R coefh[DIM], cu[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    coefh[k] = R((0.5 * dt) / d.h[k]);
+    cu[k] = R(dt / d.h[k]);
+  }
+  const int x0 = T.x0, y0 = T.y0, p0 = T.p0, p1 = T.p1;
+  const int ax = min(S.tx, g.na - x0);
+  const int by = DIM == 3 ? min(S.ty, g.nb - y0) : 1;
+  const int nint = ax * by;
+  const int tid = threadIdx.x;
+  const bool owner = tid < nint;
+  const int oa = owner ? tid % ax : 0;
+  const int ob = owner ? tid / ax : 0;
+  const bool at_x0 = (x0 == 0), at_x1 = (x0 + ax == g.na);
+  const bool at_y0 = DIM == 3 && y0 == 0, at_y1 = DIM == 3 && (y0 + by == g.nb);
+
+  const int plane = NL * S.ph * S.pw;
+  const int cplane = S.ph * S.pw;
+  const int bplane = S.bh * S.bw;
+  R* ring = smem_at<R>(smem, S.ring_off);
+  R* box = smem_at<R>(smem, S.box_off);
+  R* fa = smem_at<R>(smem, S.fa_off);
+  R* fb = smem_at<R>(smem, S.fb_off);
+  double* bs = smem_at<double>(smem, S.bs_off);
+  double* red = smem_at<double>(smem, S.red_off);
+  const int nbs = 2 * S.ty * NV + (DIM == 3 ? 2 * S.tx * NV : 0) + 2 * NV;
+  for (int e = tid; e < nbs; e += blockDim.x) bs[e] = 0.0;
+  double* bs_a = bs;                                   // [2][ty][NV]
+  double* bs_b = bs + 2 * S.ty * NV;                   // [2][tx][NV] (3D)
+  double* bs_m = bs_b + (DIM == 3 ? 2 * S.tx * NV : 0);// [2][NV]
+  const int fa_plane = S.ty * (S.tx + 1);
+  const int fb_plane = (S.ty + 1) * S.tx;
+
+  auto slot = [&](int p) { return ring + ((p - p0 + 2) % 3) * plane; };
+  HydroTile<R, DIM, VARG>::load_plane(d, g, U, gam, slot(p0 - 2), S, x0, y0, ax, by, p0 - 2);
+  HydroTile<R, DIM, VARG>::load_plane(d, g, U, gam, slot(p0 - 1), S, x0, y0, ax, by, p0 - 1);
+  HydroTile<R, DIM, VARG>::load_plane(d, g, U, gam, slot(p0), S, x0, y0, ax, by, p0);
+  __syncthreads();
+
+  R Tprev[NV], Fprev[NV], Pprev[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) Tprev[c] = Fprev[c] = Pprev[c] = R(0);
+  R gprev = gconst;
+  R wmax[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) wmax[k] = R(0);
+  bool bad = false, gate = false;
+  R* fout[3] = {(R*)d.flux_out[0], (R*)d.flux_out[1], (R*)d.flux_out[2]};
+  const bool want_flux = d.has_flux_out != 0;
+
+  // domain corners of the active box that this tile must gate (3D)
+  int ncorner = 0;
+  int corner_a[4], corner_b[4];
+  if (DIM == 3) {
+    if (at_x0 && at_y0) { corner_a[ncorner] = -1; corner_b[ncorner++] = -1; }
+    if (at_x1 && at_y0) { corner_a[ncorner] = ax; corner_b[ncorner++] = -1; }
+    if (at_x0 && at_y1) { corner_a[ncorner] = -1; corner_b[ncorner++] = by; }
+    if (at_x1 && at_y1) { corner_a[ncorner] = ax; corner_b[ncorner++] = by; }
+  }
+
+  for (int it = p0 - 1; it <= p1; ++it) {
+    const R* rm = slot(it - 1);
+    const R* rc = slot(it);
+    const R* rp = slot(it + 1);
+    const bool full = (it >= p0 && it < p1);
+    const bool edge_plane = DIM == 3 && (it == -1 || it == g.np);
+    int nring = 0, ncor = 0;
+    if (full || edge_plane) {
+      nring = DIM == 3 ? 2 * ax + 2 * by : 2;
+      ncor = ncorner;
+    }
+    const int ncell = nint + nring + ncor;
+    R Bn[NV], Tn[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) Bn[c] = Tn[c] = R(0);
+    for (int w = tid; w < ncell; w += blockDim.x) {
+      int a, b;
+      if (w < nint) {
+        a = w % ax;
+        b = w / ax;
+      } else if (w < nint + nring) {
+        const int q = w - nint;
+        if (DIM == 3) {
+          if (q < by) { a = -1; b = q; }
+          else if (q < 2 * by) { a = ax; b = q - by; }
+          else if (q < 2 * by + ax) { a = q - 2 * by; b = -1; }
+          else { a = q - 2 * by - ax; b = by; }
+        } else {
+          a = q == 0 ? -1 : ax;
+          b = 0;
+        }
+      } else {
+        const int q = w - nint - nring;
+        a = corner_a[q];
+        b = corner_b[q];
+      }
+      R ub[NV], sm[NV];
+      cell_stage<R, DIM, VARG>(rm, rc, rp, box, S, a, b, limiter, gconst, coefh, ub, sm, gate);
+      if (w < nint) {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+          Bn[c] = ub[c] - R(0.5) * sm[c];
+          Tn[c] = ub[c] + R(0.5) * sm[c];
+        }
+      }
+    }
+    __syncthreads();  // box complete; ring slot of plane it-1 free
+    if (it + 2 <= p1 + 1)
+      HydroTile<R, DIM, VARG>::load_plane(d, g, U, gam, slot(it + 2), S, x0, y0, ax, by, it + 2);
+    if (full) {
+      const int nfa = (ax + 1) * by;
+      const int nfb = DIM == 3 ? ax * (by + 1) : 0;
+      const R* bub = box;
+      const R* bsa = box + NV * bplane;
+      const R* bsb = box + 2 * NV * bplane;
+      for (int w = tid; w < nfa + nfb; w += blockDim.x) {
+        R L[NV], Rr[NV], F[NV];
+        R gl = gconst, gr = gconst;
+        if (w < nfa) {
+          const int af = w % (ax + 1), b = w / (ax + 1);
+          const int bl = (DIM == 3 ? (b + 1) * S.bw : 0) + af;  // box index of cell af-1
+#pragma unroll
+          for (int c = 0; c < NV; ++c) {
+            L[c] = bub[c * bplane + bl] + R(0.5) * bsa[c * bplane + bl];
+            Rr[c] = bub[c * bplane + bl + 1] - R(0.5) * bsa[c * bplane + bl + 1];
+          }
+          if (VARG) {
+            const int li = (DIM == 3 ? (b + 2) * S.pw : 0) + af + 1;
+            gl = rc[NV * cplane + li];
+            gr = rc[NV * cplane + li + 1];
+          }
+          hllc_cartesian<R, NV>(L, Rr, gl, gr, 0, F);
+#pragma unroll
+          for (int c = 0; c < NV; ++c) fa[c * fa_plane + b * (S.tx + 1) + af] = F[c];
+          if (af == 0 && at_x0) {
+#pragma unroll
+            for (int c = 0; c < NV; ++c) bs_a[(0 * S.ty + b) * NV + c] += (double)F[c];
+          }
+          if (af == ax && at_x1) {
+#pragma unroll
+            for (int c = 0; c < NV; ++c) bs_a[(1 * S.ty + b) * NV + c] += (double)F[c];
+          }
+          if (want_flux && fout[0]) {
+            const int64_t nf = (int64_t)g.na + 1;
+#pragma unroll
+            for (int c = 0; c < NV; ++c)
+              fout[0][((int64_t)(c * g.np + it) * g.nb + (y0 + b)) * nf + x0 + af] = F[c];
+          }
+        } else {
+          const int q = w - nfa;
+          const int a = q % ax, bf = q / ax;
+          const int bl = bf * S.bw + a + 1;  // box index of cell (a, bf-1)
+#pragma unroll
+          for (int c = 0; c < NV; ++c) {
+            L[c] = bub[c * bplane + bl] + R(0.5) * bsb[c * bplane + bl];
+            Rr[c] = bub[c * bplane + bl + S.bw] - R(0.5) * bsb[c * bplane + bl + S.bw];
+          }
+          if (VARG) {
+            const int li = (bf + 1) * S.pw + a + 2;
+            gl = rc[NV * cplane + li];
+            gr = rc[NV * cplane + li + S.pw];
+          }
+          hllc_cartesian<R, NV>(L, Rr, gl, gr, 1, F);
+#pragma unroll
+          for (int c = 0; c < NV; ++c) fb[c * fb_plane + bf * S.tx + a] = F[c];
+          if (bf == 0 && at_y0) {
+#pragma unroll
+            for (int c = 0; c < NV; ++c) bs_b[(0 * S.tx + a) * NV + c] += (double)F[c];
+          }
+          if (bf == by && at_y1) {
+#pragma unroll
+            for (int c = 0; c < NV; ++c) bs_b[(1 * S.tx + a) * NV + c] += (double)F[c];
+          }
+          if (want_flux && fout[1]) {
+#pragma unroll
+            for (int c = 0; c < NV; ++c)
+              fout[1][((int64_t)(c * g.np + it) * (g.nb + 1) + (y0 + bf)) * g.na + x0 + a] = F[c];
+          }
+        }
+      }
+    }
+    __syncthreads();  // in-plane fluxes complete; plane it+2 staged
+    R Fm[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) Fm[c] = R(0);
+    if (owner) {
+      const int li = (DIM == 3 ? (ob + 2) * S.pw : 0) + oa + 2;
+      const R gcur = VARG ? rc[NV * cplane + li] : gconst;
+      if (it >= p0) {
+        hllc_cartesian<R, NV>(Tprev, Bn, gprev, gcur, MD, Fm);
+        if (want_flux && fout[MD]) {
+#pragma unroll
+          for (int c = 0; c < NV; ++c)
+            fout[MD][((int64_t)(c * (g.np + 1) + it) * g.nb + (y0 + ob)) * g.na + x0 + oa] = Fm[c];
+        }
+        if (it > p0) {
+          R un[NV];
+#pragma unroll
+          for (int c = 0; c < NV; ++c) un[c] = Pprev[c] - cu[MD] * (Fm[c] - Fprev[c]);
+          const int64_t off = (int64_t)(it - 1) * g.ps + (int64_t)(y0 + ob) * g.na + (x0 + oa);
+#pragma unroll
+          for (int c = 0; c < NV; ++c) Un[c * g.cs + off] = un[c];
+          if (!physical_cell<R, NV>(un)) bad = true;
+          R w[DIM];
+          wave_speeds<R, DIM>(un, gprev, w);
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) wmax[k] = fmax(wmax[k], w[k]);
+        }
+#pragma unroll
+        for (int c = 0; c < NV; ++c) Fprev[c] = Fm[c];
+      }
+      if (full) {
+        const int fi = ob * (S.tx + 1) + oa;
+#pragma unroll
+        for (int c = 0; c < NV; ++c)
+          Pprev[c] = rc[c * cplane + li] - cu[0] * (fa[c * fa_plane + fi + 1] - fa[c * fa_plane + fi]);
+        if (DIM == 3) {
+          const int gi = ob * S.tx + oa;
+#pragma unroll
+          for (int c = 0; c < NV; ++c)
+            Pprev[c] = Pprev[c] - cu[1] * (fb[c * fb_plane + gi + S.tx] - fb[c * fb_plane + gi]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NV; ++c) Tprev[c] = Tn[c];
+      gprev = gcur;
+    }
+    if (it >= p0 && (it == 0 || it == g.np)) {  // march-axis boundary faces
+      const int side = it == 0 ? 0 : 1;
+#pragma unroll
+      for (int c = 0; c < NV; ++c) {
+        const double s = block_sum(owner ? (double)Fm[c] : 0.0, red);
+        if (tid == 0) bs_m[side * NV + c] += s;
+      }
+    }
+  }
+
+  // tile epilogue: flags, wave maxima, boundary sums
+  int fl = (bad ? kFlagNonphysical : 0) | (gate ? kFlagGate : 0);
+  fl = block_or(fl, reinterpret_cast<int*>(red));
+  double wm[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) wm[k] = block_max(owner ? (double)wmax[k] : 0.0, red);
+  __syncthreads();
+  if (tid == 0) {
+    double* out = A.t_bsum + (size_t)t * 15;
+    for (int c = 0; c < NV; ++c) {
+      double sa = 0.0;
+      for (int b = 0; b < S.ty; ++b) sa += bs_a[(1 * S.ty + b) * NV + c] - bs_a[(0 * S.ty + b) * NV + c];
+      out[0 * 5 + c] = sa;
+      if (DIM == 3) {
+        double sb = 0.0;
+        for (int a = 0; a < S.tx; ++a) sb += bs_b[(1 * S.tx + a) * NV + c] - bs_b[(0 * S.tx + a) * NV + c];
+        out[1 * 5 + c] = sb;
+      }
+      out[MD * 5 + c] = bs_m[NV + c] - bs_m[c];
+    }
+    for (int k = 0; k < DIM; ++k) A.t_wmax[(size_t)t * 3 + k] = wm[k];
+    A.t_flags[t] = fl;
+    if (fl & (kFlagNonphysical | kFlagGate)) atomicOr(&st.fb_word, fl);
+  }
+  __syncthreads();
+}
+
+template <typename R, int DIM, bool VARG>
+__global__ void __launch_bounds__(256) hydro_kernel(StepArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  HydroSmem<R, DIM, VARG> S;
+  S.init(A.tx, A.ty);
+  for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) hydro_tile<R, DIM, VARG>(A, t, smem, S);
+}
+
+// --------------------------------------------------------------------------
+// First-order fallback (whole step), run only when a tile flagged the
+// instance.  3D: Rusanov on padded cells (python/cfdSolver/torchSolver3D.py:
+// 162-176); 2D: LLF with floored primitives (torchSolver2D.py:419-462).
+// --------------------------------------------------------------------------
+template <typename R, int DIM>
+__device__ __forceinline__ void first_order_face(const R* L, const R* Rr, R gl, R gr, int dd,
+                                                 R* F) {
+  constexpr int NV = DIM + 2;
+  if (DIM == 3) {
+    const int m = dd + 1;
+    R fl[NV], fr[NV];
+    flux3<R>(L, gl, m, fl);
+    flux3<R>(Rr, gr, m, fr);
+    const R sl_ = (L[1] * L[1] + L[2] * L[2]) + L[3] * L[3];
+    const R sr_ = (Rr[1] * Rr[1] + Rr[2] * Rr[2]) + Rr[3] * Rr[3];
+    const R pl = (gl - R(1)) * (L[4] - (R(0.5) * sl_) / L[0]);
+    const R pr = (gr - R(1)) * (Rr[4] - (R(0.5) * sr_) / Rr[0]);
+    const R speed = np_max(fabs(L[m] / L[0]) + sqrt((gl * pl) / L[0]),
+                           fabs(Rr[m] / Rr[0]) + sqrt((gr * pr) / Rr[0]));
+#pragma unroll
+    for (int c = 0; c < NV; ++c) F[c] = R(0.5) * ((fl[c] + fr[c]) - speed * (Rr[c] - L[c]));
+  } else {
+    R f[2][NV], cs[2];
+    const R* uu[2] = {L, Rr};
+    const R gg[2] = {gl, gr};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const R* u = uu[k];
+      const R rho = np_max(u[0], R(kFloor));
+      const R ux = u[1] / rho;
+      const R vy = u[2] / rho;
+      const R p = np_max((gg[k] - R(1)) * (u[3] - (R(0.5) * rho) * (ux * ux + vy * vy)), R(kFloor));
+      const R snd = sqrt((gg[k] * np_max(p, R(kFloor))) / np_max(rho, R(kFloor)));
+      const R vn = dd == 0 ? ux : vy;
+      if (dd == 0) {
+        f[k][0] = u[1];
+        f[k][1] = u[1] * ux + p;
+        f[k][2] = u[2] * ux;
+        f[k][3] = ux * (u[3] + p);
+      } else {
+        f[k][0] = u[2];
+        f[k][1] = u[1] * vy;
+        f[k][2] = u[2] * vy + p;
+        f[k][3] = vy * (u[3] + p);
+      }
+      cs[k] = fabs(vn) + snd;
+    }
+    const R speed = np_max(cs[0], cs[1]);
+#pragma unroll
+    for (int c = 0; c < NV; ++c) F[c] = R(0.5) * ((f[0][c] + f[1][c]) - speed * (Rr[c] - L[c]));
+  }
+}
+
+template <typename R, int DIM, bool VARG>
+__global__ void __launch_bounds__(256) fallback_kernel(StepArgs A) {
+  constexpr int NV = DIM + 2;
+  __shared__ double red[40];
+  for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
+    const Tile T = A.tiles[t];
+    const InstDesc& d = A.desc[T.inst];
+    InstState& st = A.st[T.inst];
+    if (st.status != kReady || st.fb_word == 0) continue;  // uniform
+    Geo<DIM> g;
+    g.init(d);
+    const int src = (st.cur + A.src_off) % d.nring;
+    const int dst = (st.cur + A.dst_off) % d.nring;
+    const R* U = (const R*)d.U[src];
+    R* Un = (R*)d.U[dst];
+    const R* gam = VARG ? (const R*)d.gam : nullptr;
+    const double dt = st.dt;
+    R cu[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) cu[k] = R(dt / d.h[k]);
+    const int ax = min(A.tx, g.na - T.x0);
+    const int by = DIM == 3 ? min(A.ty, g.nb - T.y0) : 1;
+    const bool owner = (int)threadIdx.x < ax * by;
+    const int a = T.x0 + (owner ? (int)threadIdx.x % ax : 0);
+    const int b = DIM == 3 ? T.y0 + (owner ? (int)threadIdx.x / ax : 0) : 0;
+    double acc[DIM][NV];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+#pragma unroll
+      for (int c = 0; c < NV; ++c) acc[k][c] = 0.0;
+    R wmax[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) wmax[k] = R(0);
+    bool bad = false;
+    R* fout[3] = {(R*)d.flux_out[0], (R*)d.flux_out[1], (R*)d.flux_out[2]};
+    if (owner) {
+      for (int p = T.p0; p < T.p1; ++p) {
+        R u[NV], un[NV];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+          u[c] = fetch_padded<R, DIM>(d, g, U, gam, c, a, b, p);
+          un[c] = u[c];
+        }
+        const R gc = VARG ? fetch_padded<R, DIM>(d, g, U, gam, NV, a, b, p) : R(d.gamma);
+#pragma unroll
+        for (int dd = 0; dd < DIM; ++dd) {
+          const int ia = dd == 0 ? 1 : 0;
+          const int ib = (DIM == 3 && dd == 1) ? 1 : 0;
+          const int ip = dd == DIM - 1 ? 1 : 0;
+          R lo[NV], hi[NV], Fm[NV], Fp[NV];
+#pragma unroll
+          for (int c = 0; c < NV; ++c) {
+            lo[c] = fetch_padded<R, DIM>(d, g, U, gam, c, a - ia, b - ib, p - ip);
+            hi[c] = fetch_padded<R, DIM>(d, g, U, gam, c, a + ia, b + ib, p + ip);
+          }
+          const R glo = VARG ? fetch_padded<R, DIM>(d, g, U, gam, NV, a - ia, b - ib, p - ip) : gc;
+          const R ghi = VARG ? fetch_padded<R, DIM>(d, g, U, gam, NV, a + ia, b + ib, p + ip) : gc;
+          first_order_face<R, DIM>(lo, u, glo, gc, dd, Fm);
+          first_order_face<R, DIM>(u, hi, gc, ghi, dd, Fp);
+#pragma unroll
+          for (int c = 0; c < NV; ++c) un[c] = un[c] - cu[dd] * (Fp[c] - Fm[c]);
+          const int idx = dd == 0 ? a : (dd == DIM - 1 ? p : b);
+          const int n = dd == 0 ? g.na : (dd == DIM - 1 ? g.np : g.nb);
+          if (idx == 0) {
+#pragma unroll
+            for (int c = 0; c < NV; ++c) acc[dd][c] -= (double)Fm[c];
+          }
+          if (idx == n - 1) {
+#pragma unroll
+            for (int c = 0; c < NV; ++c) acc[dd][c] += (double)Fp[c];
+          }
+          if (d.has_flux_out && fout[dd]) {
+            // face arrays: the axis dd has n+1 faces
+            const int fa_n = dd == 0 ? g.na + 1 : g.na;
+            const int fb_n = (DIM == 3 && dd == 1) ? g.nb + 1 : g.nb;
+            const int fp_n = dd == DIM - 1 ? g.np + 1 : g.np;
+            (void)fp_n;
+#pragma unroll
+            for (int c = 0; c < NV; ++c) {
+              const int64_t base = (int64_t)c * (dd == DIM - 1 ? g.np + 1 : g.np);
+              fout[dd][((base + p) * fb_n + b) * fa_n + a] = Fm[c];
+              if (idx == n - 1)
+                fout[dd][((base + p + ip) * fb_n + b + ib) * fa_n + a + ia] = Fp[c];
+            }
+          }
+        }
+        const int64_t off = (int64_t)p * g.ps + (int64_t)b * g.na + a;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) Un[c * g.cs + off] = un[c];
+        if (!physical_cell<R, NV>(un)) bad = true;
+        R w[DIM];
+        wave_speeds<R, DIM>(un, gc, w);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) wmax[k] = fmax(wmax[k], w[k]);
+      }
+    }
+    int fl = block_or(bad ? kFlagNonphysical : 0, reinterpret_cast<int*>(red));
+    double sums[DIM][NV];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+#pragma unroll
+      for (int c = 0; c < NV; ++c) sums[k][c] = block_sum(acc[k][c], red);
+    double wm[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) wm[k] = block_max(owner ? (double)wmax[k] : 0.0, red);
+    if (threadIdx.x == 0) {
+      double* out = A.t_bsum + (size_t)t * 15;
+      for (int k = 0; k < DIM; ++k)
+        for (int c = 0; c < NV; ++c) out[k * 5 + c] = sums[k][c];
+      for (int k = 0; k < DIM; ++k) A.t_wmax[(size_t)t * 3 + k] = wm[k];
+      A.t_flags[t] = fl;
+    }
+    __syncthreads();
+  }
+}
+
+// --------------------------------------------------------------------------
+// Wave-speed maxima of the current state (initial / re-planned dt).
+// --------------------------------------------------------------------------
+template <typename R, int DIM, bool VARG>
+__global__ void __launch_bounds__(256) waves_kernel(StepArgs A) {
+  constexpr int NV = DIM + 2;
+  __shared__ double red[40];
+  for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
+    const Tile T = A.tiles[t];
+    const InstDesc& d = A.desc[T.inst];
+    const InstState& st = A.st[T.inst];
+    Geo<DIM> g;
+    g.init(d);
+    const R* U = (const R*)d.U[(st.cur + A.src_off) % d.nring];
+    const R* gam = VARG ? (const R*)d.gam : nullptr;
+    const int ax = min(A.tx, g.na - T.x0);
+    const int by = DIM == 3 ? min(A.ty, g.nb - T.y0) : 1;
+    const bool owner = (int)threadIdx.x < ax * by;
+    const int a = T.x0 + (owner ? (int)threadIdx.x % ax : 0);
+    const int b = DIM == 3 ? T.y0 + (owner ? (int)threadIdx.x / ax : 0) : 0;
+    R wmax[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) wmax[k] = R(0);
+    bool bad = false;
+    double sum[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) sum[c] = 0.0;
+    if (owner) {
+      for (int p = T.p0; p < T.p1; ++p) {
+        const int64_t off = (int64_t)p * g.ps + (int64_t)b * g.na + a;
+        R u[NV];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+          u[c] = U[c * g.cs + off];
+          sum[c] += (double)u[c];
+        }
+        const R gc = VARG ? gam[off] : R(d.gamma);
+        if (!physical_cell<R, NV>(u)) bad = true;
+        R w[DIM];
+        wave_speeds<R, DIM>(u, gc, w);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) wmax[k] = fmax(wmax[k], w[k]);
+      }
+    }
+    int fl = block_or(bad ? kFlagNonphysical : 0, reinterpret_cast<int*>(red));
+    double wm[DIM], sm[NV];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) wm[k] = block_max(owner ? (double)wmax[k] : 0.0, red);
+#pragma unroll
+    for (int c = 0; c < NV; ++c) sm[c] = block_sum(sum[c], red);
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < DIM; ++k) A.t_wmax[(size_t)t * 3 + k] = wm[k];
+      for (int c = 0; c < NV; ++c) A.t_sum[(size_t)t * 5 + c] = sm[c];
+      A.t_flags[t] = fl;
+    }
+    __syncthreads();
+  }
+}
+
+// --------------------------------------------------------------------------
+// Per-instance finalize: commit the step (ring swap, boundary integral,
+// time, steps), then plan the next dt (python/cfdSolver/torchSession.py:
+// 379-396, 498-522).  mode 0: commit + plan; 1: plan only; 2: integrals only;
+// 3: record the initial integrals, then plan (bind).  One CTA per instance.
+// --------------------------------------------------------------------------
+__device__ __forceinline__ void plan_next(const InstDesc& d, InstState& st, const double* w,
+                                          int fp32) {
+  if (st.time == d.t_end) {
+    st.status = kDone;
+    return;
+  }
+  if (st.steps >= d.max_steps) {
+    st.status = kErrMaxSteps;
+    return;
+  }
+  double dt;
+  if (d.dim == 3) {
+    const double total = (w[0] / d.h[0] + w[1] / d.h[1]) + w[2] / d.h[2];
+    dt = d.cfl / total;
+  } else if (d.dim == 2) {
+    double w0 = w[0], w1 = w[1];
+    if (d.bc[1] == kBcInflow) {  // the inlet ghost rows take part in the 2D dt
+      const double rho = fmax(d.inlet[0], 1e-12);
+      const double ux = d.inlet[1] / rho, vy = d.inlet[2] / rho;
+      const double p = fmax((1.4 - 1.0) * (d.inlet[3] - (0.5 * rho) * (ux * ux + vy * vy)), 1e-12);
+      const double a = sqrt((1.4 * fmax(p, 1e-12)) / fmax(rho, 1e-12));
+      w0 = fmax(w0, fabs(ux) + a);
+      w1 = fmax(w1, fabs(vy) + a);
+    }
+    const double total = w0 / d.h[0] + w1 / d.h[1];
+    dt = total <= 1e-12 ? 1e-3 : d.cfl / total;
+  } else {
+    // 1D: w[0] = max |S| over faces, w[1] = max(|u| + a) over padded cells
+    const double dw = w[0] > 0 ? (d.cfl * d.h[0]) / w[0] : 1e-6;
+    const double dh = d.cfl * d.h[0] / w[1];
+    dt = dh < dw ? dh : dw;
+  }
+  if (fp32) dt = (double)(float)dt;
+  const double rem = d.t_end - st.time;
+  if (rem < dt) dt = rem;
+  st.dt = dt;
+  if (!isfinite(dt) || dt <= 0.0 || st.time + dt == st.time) {
+    st.status = kErrStall;
+    return;
+  }
+  st.status = kReady;
+}
+
+#ifdef TFV_DEFINE_SHARED_KERNELS  // defined by exactly one translation unit
+__global__ void __launch_bounds__(256) finalize_kernel(StepArgs A, int mode, int fp32,
+                                                       double* integrals_out) {
+  __shared__ double red[40];
+  __shared__ double sh_w[3], sh_s[15], sh_i[5];
+  __shared__ int sh_f;
+  const int i = blockIdx.x;
+  if (i >= A.ninst) return;
+  const InstDesc& d = A.desc[i];
+  InstState& st = A.st[i];
+  if (mode == 0 && st.status != kReady) return;  // uniform
+  const int nv = d.dim + 2;
+  int fl = 0;
+  double w[3] = {0.0, 0.0, 0.0};
+  double s[15], isum[5];
+  for (int k = 0; k < 15; ++k) s[k] = 0.0;
+  for (int k = 0; k < 5; ++k) isum[k] = 0.0;
+  for (int t = d.tile0 + threadIdx.x; t < d.tile0 + d.ntiles; t += blockDim.x) {
+    fl |= A.t_flags[t];
+    for (int k = 0; k < 3; ++k) w[k] = fmax(w[k], A.t_wmax[(size_t)t * 3 + k]);
+    if (mode == 0)
+      for (int k = 0; k < 15; ++k) s[k] += A.t_bsum[(size_t)t * 15 + k];
+    if (mode >= 2)
+      for (int k = 0; k < 5; ++k) isum[k] += A.t_sum[(size_t)t * 5 + k];
+  }
+  fl = block_or(fl, reinterpret_cast<int*>(red));
+  if (threadIdx.x == 0) sh_f = fl;
+  for (int k = 0; k < 3; ++k) {
+    const double v = block_max(w[k], red);
+    if (threadIdx.x == 0) sh_w[k] = v;
+  }
+  if (mode == 0) {
+    for (int k = 0; k < 15; ++k) {
+      const double v = block_sum(s[k], red);
+      if (threadIdx.x == 0) sh_s[k] = v;
+    }
+  }
+  if (mode >= 2) {
+    for (int k = 0; k < 5; ++k) {
+      const double v = block_sum(isum[k], red);
+      if (threadIdx.x == 0) sh_i[k] = v;
+    }
+  }
+  if (threadIdx.x != 0) return;
+  if (mode == 2) {
+    for (int c = 0; c < 5; ++c) integrals_out[i * 5 + c] = c < nv ? sh_i[c] * d.vol : 0.0;
+    return;
+  }
+  if (mode == 3) {
+    for (int c = 0; c < 5; ++c) st.initial[c] = c < nv ? sh_i[c] * d.vol : 0.0;
+  }
+  if (mode == 0) {
+    if (sh_f & kFlagNonphysical) {
+      st.status = kErrNonphysical;
+      st.fb_word = 0;
+      return;
+    }
+    if (sh_f & kFlagSpecies) {
+      st.status = kErrSpecies;
+      st.fb_word = 0;
+      return;
+    }
+    const double dt = st.dt;
+    for (int c = 0; c < nv; ++c) {
+      double out = 0.0;
+      for (int k = 0; k < d.dim; ++k) out += dt * d.vol / d.h[k] * sh_s[k * 5 + c];
+      st.boundary[c] += out;
+    }
+    st.cur = (st.cur + A.dst_off) % d.nring;
+    const double tn = st.time + dt;
+    st.time = tn < d.t_end ? tn : d.t_end;
+    st.steps += 1;
+    st.last_fallback = st.fb_word != 0;
+    st.fallback_steps += st.fb_word != 0;
+    st.fb_word = 0;
+    st.retry = 0;
+  } else if (st.status != kReady && st.status != kDone) {
+    return;  // plan-only keeps a pending error
+  }
+  plan_next(d, st, sh_w, fp32);
+}
+
+#endif  // TFV_DEFINE_SHARED_KERNELS
+
+// --------------------------------------------------------------------------
+// Stateless HLLC over n faces (python/cfdSolver/torchFlux.py:125-248).
+// --------------------------------------------------------------------------
+template <typename R, int NV>
+__global__ void hllc_faces_kernel(int64_t n, const R* ul, const R* ur, const R* gl, const R* gr,
+                                  R* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    R a[NV], b[NV], f[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+      a[c] = ul[c * n + i];
+      b[c] = ur[c * n + i];
+    }
+    hllc<R, NV - 3>(a, b, gl[i], gr[i], f);
+#pragma unroll
+    for (int c = 0; c < NV; ++c) out[c * n + i] = f[c];
+  }
+}
+
+}  // namespace tfv

@@ -1,0 +1,27 @@
+// Launchers exported by the per-precision translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "tfv_types.h"
+
+namespace tfv {
+
+enum : int { kOpHydro = 0, kOpFallback = 1, kOpWaves = 2 };
+
+cudaError_t launch_step_f64(int op, int dim, bool varg, const StepArgs& A, int grid, int block,
+                            cudaStream_t s);
+cudaError_t launch_step_f32(int op, int dim, bool varg, const StepArgs& A, int grid, int block,
+                            cudaStream_t s);
+size_t hydro_smem_f64(int dim, bool varg, int tx, int ty);
+size_t hydro_smem_f32(int dim, bool varg, int tx, int ty);
+cudaError_t launch_hllc_f64(int nv, int64_t n, const void* ul, const void* ur, const void* gl,
+                            const void* gr, void* out, cudaStream_t s);
+cudaError_t launch_hllc_f32(int nv, int64_t n, const void* ul, const void* ur, const void* gl,
+                            const void* gr, void* out, cudaStream_t s);
+cudaError_t launch_finalize(const StepArgs& A, int mode, int fp32, double* integrals_out,
+                            cudaStream_t s);
+
+}  // namespace tfv

@@ -1,0 +1,262 @@
+// Device physics of TORCH's Cartesian finite-volume step, templated on the
+// arithmetic type R (double: reference-faithful path; float: bulk FP32 path).
+//
+// Every expression keeps the operation order of the NumPy reference so that
+// the double instantiation, compiled without FMA contraction (-fmad=false),
+// reproduces the reference bit for bit: `a * b * c` in Python is (a*b)*c,
+// sums of squares over the component axis are sequential, masks follow the
+// reference's precedence.  The float instantiation uses the same formulas
+// with contraction and fast division allowed by its compile flags.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tfv {
+
+constexpr double kFloor = 1e-12;  // density / pressure floor
+constexpr double kGuard = 1e-14;  // division guard (limiters, HLLC)
+
+// numpy.maximum / numpy.minimum: NaN propagates, first operand wins ties.
+template <typename R>
+__device__ __forceinline__ R np_max(R a, R b) { return (a >= b || a != a) ? a : b; }
+template <typename R>
+__device__ __forceinline__ R np_min(R a, R b) { return (a <= b || a != a) ? a : b; }
+
+// np.where(abs(x) < g, g, x)
+template <typename R>
+__device__ __forceinline__ R guarded(R x, R g) { return (fabs(x) < g) ? g : x; }
+
+template <typename R>
+__device__ __forceinline__ bool finite_(R x) { return isfinite(x); }
+
+// --------------------------------------------------------------------------
+// Limiters.
+// 3D: python/cfdSolver/torchSolver3D.py:86-111.
+// 2D: python/cfdSolver/torchSolver2D.py:124-168 (VanLeer/Albada zero for
+//     r <= 0, Unos without the (1+2r)/3 bound).
+// --------------------------------------------------------------------------
+template <typename R, int DIM>
+__device__ __forceinline__ R limited_slope(R um, R uc, R up, int limiter) {
+  const R minus = uc - um;
+  const R plus = up - uc;
+  const R r = minus / guarded(plus, R(kGuard));
+  R phi;
+  switch (limiter) {
+    case 1: {  // Albada
+      const R pos = np_max(r, R(0));
+      phi = (pos * pos + pos) / (pos * pos + R(1));
+      if (DIM == 2 && !(r > R(0))) phi = R(0);
+      break;
+    }
+    case 2:  // MINBEE
+      phi = np_max(R(0), np_min(r, R(1)));
+      break;
+    case 3:  // Superbee
+      phi = np_max(R(0), np_max(np_min(R(2) * r, R(1)), np_min(r, R(2))));
+      break;
+    case 4:  // Unos
+      if (DIM == 3)
+        phi = np_max(R(0), np_min(np_min(np_min(R(2), R(2) * r), (R(2) + r) / R(3)),
+                                  (R(1) + R(2) * r) / R(3)));
+      else
+        phi = np_max(R(0), np_min(np_min(R(2), R(2) * r), (R(2) + r) / R(3)));
+      break;
+    default: {  // VanLeer
+      const R pos = np_max(r, R(0));
+      phi = (R(2) * pos) / (R(1) + pos);
+      if (DIM == 2 && !(r > R(0))) phi = R(0);
+      break;
+    }
+  }
+  return phi * plus;
+}
+
+// --------------------------------------------------------------------------
+// Predictor fluxes.
+// 3D _flux: python/cfdSolver/torchSolver3D.py:77-83 with uconsv_to_uprim_3d
+//   (:37-44, no floors).  m = normal momentum row (1..3).
+// 2D euler_flux_x / euler_flux_y: python/cfdSolver/torchSolver2D.py:326-352
+//   (rho and p floored).
+// --------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void flux3(const R* u, R g, int m, R* f) {
+  const R rho = u[0];
+  const R ssum = (u[1] * u[1] + u[2] * u[2]) + u[3] * u[3];
+  const R p = (g - R(1)) * (u[4] - (R(0.5) * ssum) / rho);
+  const R vel = u[m] / rho;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) f[c] = u[c] * vel;
+  f[m] = f[m] + p;
+  f[4] = vel * (u[4] + p);
+}
+
+template <typename R>
+__device__ __forceinline__ void flux2(const R* u, R g, int normal, R* f) {
+  const R rho = np_max(u[0], R(kFloor));
+  const R vx = u[1] / rho;
+  const R vy = u[2] / rho;
+  const R p = np_max((g - R(1)) * (u[3] - (R(0.5) * rho) * (vx * vx + vy * vy)), R(kFloor));
+  if (normal == 0) {
+    f[0] = rho * vx;
+    f[1] = rho * (vx * vx) + p;
+    f[2] = (rho * vx) * vy;
+    f[3] = vx * (u[3] + p);
+  } else {
+    f[0] = rho * vy;
+    f[1] = (rho * vx) * vy;
+    f[2] = rho * (vy * vy) + p;
+    f[3] = vy * (u[3] + p);
+  }
+}
+
+// Physical-state test of one cell (python/cfdSolver/torchSolver.py:1038-1046).
+template <typename R, int NV>
+__device__ __forceinline__ bool physical_cell(const R* u) {
+  bool ok = true;
+#pragma unroll
+  for (int c = 0; c < NV; ++c) ok = ok && finite_(u[c]);
+  R s = u[1] * u[1];
+#pragma unroll
+  for (int c = 2; c < NV - 1; ++c) s = s + u[c] * u[c];
+  return ok && (u[0] > R(kFloor)) && (u[NV - 1] - (R(0.5) * s) / u[0] > R(kFloor));
+}
+
+// --------------------------------------------------------------------------
+// HLLC in the normal basis: rows rho, m_n, m_t[NT], E
+// (python/cfdSolver/torchFlux.py:125-248).  Only the star state of the side
+// that can be selected is formed; values are identical to evaluating both.
+// Where no wave-speed mask holds (NaN speeds) the result is NaN.
+// --------------------------------------------------------------------------
+template <typename R, int NT>
+__device__ __forceinline__ void hllc(const R* ul, const R* ur, R gl, R gr, R* out) {
+  constexpr int NV = NT + 3;
+  constexpr int E = NV - 1;
+  const R g = R(0.5) * (gl + gr);
+  const R rl = np_max(ul[0], R(kFloor));
+  const R rr = np_max(ur[0], R(kFloor));
+  const R unl = ul[1] / rl;
+  const R unr = ur[1] / rr;
+  R utl[NT], utr[NT];
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
+    utl[t] = ul[2 + t] / rl;
+    utr[t] = ur[2 + t] / rr;
+  }
+  R stl = utl[0] * utl[0], str = utr[0] * utr[0];
+#pragma unroll
+  for (int t = 1; t < NT; ++t) {
+    stl = stl + utl[t] * utl[t];
+    str = str + utr[t] * utr[t];
+  }
+  const R kel = (R(0.5) * rl) * (unl * unl + stl);
+  const R ker = (R(0.5) * rr) * (unr * unr + str);
+  const R pl = np_max((gl - R(1)) * (ul[E] - kel), R(kFloor));
+  const R pr = np_max((gr - R(1)) * (ur[E] - ker), R(kFloor));
+  const R al = sqrt((gl * pl) / rl);
+  const R ar = sqrt((gr * pr) / rr);
+
+  R fl[NV], fr[NV];
+  fl[0] = rl * unl;
+  fl[1] = rl * (unl * unl) + pl;
+  fr[0] = rr * unr;
+  fr[1] = rr * (unr * unr) + pr;
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
+    fl[2 + t] = (rl * unl) * utl[t];
+    fr[2 + t] = (rr * unr) * utr[t];
+  }
+  fl[E] = unl * (ul[E] + pl);
+  fr[E] = unr * (ur[E] + pr);
+
+  const R sql = sqrt(rl);
+  const R sqr = sqrt(rr);
+  const R inv = R(1) / (sql + sqr);
+  const R uroe = (sql * unl + sqr * unr) * inv;
+  R vsum;
+  {
+    const R v0 = (sql * utl[0] + sqr * utr[0]) * inv;
+    vsum = v0 * v0;
+#pragma unroll
+    for (int t = 1; t < NT; ++t) {
+      const R vt = (sql * utl[t] + sqr * utr[t]) * inv;
+      vsum = vsum + vt * vt;
+    }
+  }
+  const R hl = (ul[E] + pl) / rl;
+  const R hr = (ur[E] + pr) / rr;
+  const R hroe = (sql * hl + sqr * hr) * inv;
+  const R keroe = R(0.5) * (uroe * uroe + vsum);
+  const R aroe = sqrt(np_max((g - R(1)) * (hroe - keroe), R(kFloor)));
+
+  const R sL = np_min(unl - al, uroe - aroe);
+  const R sR = np_max(unr + ar, uroe + aroe);
+  const R den = guarded(rl * (sL - unl) - rr * (sR - unr), R(kGuard));
+  const R ss = (((pr - pl) + (rl * unl) * (sL - unl)) - (rr * unr) * (sR - unr)) / den;
+
+  // star state of the side whose star region can be selected
+  const bool right = (ss <= R(0));
+  const R* u = right ? ur : ul;
+  const R* fs = right ? fr : fl;
+  const R rho = right ? rr : rl;
+  const R un = right ? unr : unl;
+  const R p = right ? pr : pl;
+  const R s = right ? sR : sL;
+  const R dss = guarded(s - ss, R(kGuard));
+  const R rho_s = np_max(rho * ((s - un) / dss), R(kFloor));
+  const R dun = guarded(s - un, R(kGuard));
+  R star[NV];
+  star[0] = rho_s;
+  star[1] = rho_s * ss;
+#pragma unroll
+  for (int t = 0; t < NT; ++t) star[2 + t] = rho_s * (right ? utr[t] : utl[t]);
+  star[E] = rho_s * (u[E] / rho + (ss - un) * (ss + p / (rho * dun)));
+  const bool close = fabs(s - ss) < R(kFloor);
+
+  const bool mr = (R(0) >= sR);
+  const bool msr = (ss <= R(0)) && (R(0) <= sR);
+  const bool msl = (sL <= R(0)) && (R(0) <= ss);
+  const bool ml = (R(0) <= sL);
+#pragma unroll
+  for (int c = 0; c < NV; ++c) {
+    const R fstar = close ? fs[c] : fs[c] + s * (star[c] - u[c]);
+    R v = R(NAN);
+    if (ml) v = fl[c];
+    if (msl || msr) v = fstar;
+    if (mr) v = fr[c];
+    out[c] = v;
+  }
+}
+
+// Rotation into the normal basis (python/cfdSolver/torchFlux.py:36-39):
+// order = [0, normal] + other momenta ascending + [E].
+template <int NV>
+__device__ __forceinline__ void normal_order(int normal, int* order) {
+  order[0] = 0;
+  order[1] = normal;
+  int k = 2;
+#pragma unroll
+  for (int m = 1; m < NV - 1; ++m)
+    if (m != normal) order[k++] = m;
+  order[NV - 1] = NV - 1;
+}
+
+// HLLC across a face along direction d (0=x,1=y,2=z) with Cartesian inputs
+// and output (python/cfdSolver/torchFlux.py:6-77 without the batching).
+template <typename R, int NV>
+__device__ __forceinline__ void hllc_cartesian(const R* L, const R* Rt, R gl, R gr, int d,
+                                               R* F) {
+  int order[NV];
+  normal_order<NV>(d + 1, order);
+  R ul[NV], ur[NV], f[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) {
+    ul[c] = L[order[c]];
+    ur[c] = Rt[order[c]];
+  }
+  hllc<R, NV - 3>(ul, ur, gl, gr, f);
+#pragma unroll
+  for (int c = 0; c < NV; ++c) F[order[c]] = f[c];
+}
+
+}  // namespace tfv

@@ -1,0 +1,424 @@
+"""GPU drop-in for TORCH's Cartesian ``Simulation`` session.
+
+Mirrors python/cfdSolver/torchSession.py:19-694 for Cartesian uniform grids
+(the ``uses_metric_kernel == False`` branch of ``Simulation.step``): same
+constructor keywords, state layout ``(dim+2, nz, ny, nx)`` x fastest,
+properties, transactional ``step()`` and exception types.  The state lives on
+the GPU; ``state``, ``lam`` and ``beta`` materialise as host float64 arrays on
+access so that host-side consumers (checkpoint writers, plots) keep working.
+
+Extensions (off by default): ``precision="fp32"`` runs the bulk step in FP32
+with FP64 time and conservation sums; ``strict_cfl=False`` accepts CFL > 0.5
+(rejected by the reference's validate_grid, torchSolver.py:1074-1088);
+``chemistry=`` selects the nondimensional Arrhenius closure.
+"""
+
+import ctypes as C
+import uuid
+
+import numpy as np
+import torch
+
+from . import _lib
+
+LIMITERS = ("VanLeer", "Albada", "MINBEE", "Superbee", "Unos")
+DEFAULT_INLET = [1.0, 0.0, 100.0, 101325.0]
+SI_CHEMISTRY = dict(q_heat=141584000.0, activation_energy=17.15 * 4184.0,
+                    pre_exponential=1.76e5)
+
+
+def _validate_grid(length, cells, cfl, end_time, strict_cfl):
+    """validate_grid (python/cfdSolver/torchSolver.py:1074-1088)."""
+    cfl_ok = 0 < cfl <= 0.5 if strict_cfl else 0 < cfl <= 1.0
+    if (not isinstance(cells, (int, np.integer)) or not np.isfinite([length, cfl, end_time]).all()
+            or length <= 0 or cells < 2 or not cfl_ok or end_time < 0):
+        raise ValueError("Require length > 0, cells >= 2, 0 < CFL <= 0.5 and final time >= 0")
+
+
+def _physical(state):
+    """physical_state (python/cfdSolver/torchSolver.py:1038-1046)."""
+    return bool(np.isfinite(state).all() and np.all(state[0] > 1e-12) and np.all(
+        state[-1] - 0.5 * np.sum(state[1:-1] ** 2, axis=0) / state[0] > 1e-12))
+
+
+def prim_to_cons(primitive, gamma):
+    """Session primitive -> conservative conversion (torchSession.py:145-150)."""
+    state = primitive.copy()
+    state[1:-1] *= primitive[0]
+    state[-1] = primitive[-1] / (gamma - 1) + 0.5 * primitive[0] * np.sum(
+        primitive[1:-1] ** 2, axis=0)
+    return state
+
+
+def make_config(dim, counts, lengths, boundaries, *, t_end, cfl, gamma, limiter, max_steps,
+                reactive=False, kinetic_model="arrhenius", closure="si", chemistry=None,
+                inlet_primitive=None, controller="Sound Speed Controlled",
+                variant="Variante 1 - Original", wavespeed="Pressure Based"):
+    cfg = _lib.Config()
+    cfg.dim = dim
+    for k in range(3):
+        cfg.counts[k] = int(counts[k]) if k < dim else 1
+        cfg.lengths[k] = float(lengths[k]) if k < dim else 1.0
+        cfg.bc[k] = _lib.bc_code(boundaries[k]) if k < dim else 0
+    cfg.limiter = _lib.LIMITERS[limiter]
+    cfg.gamma = float(gamma)
+    cfg.cfl = float(cfl)
+    cfg.t_end = float(t_end)
+    cfg.max_steps = int(max_steps)
+    cfg.reactive = int(bool(reactive))
+    cfg.kinetic_model = _lib.MODELS[kinetic_model]
+    cfg.closure = _lib.CLOSURES[closure]
+    chem = dict(SI_CHEMISTRY)
+    chem.update(chemistry or {})
+    cfg.q_heat = chem["q_heat"]
+    cfg.activation = chem["activation_energy"]
+    cfg.pre_exponential = chem["pre_exponential"]
+    inlet = DEFAULT_INLET if inlet_primitive is None else inlet_primitive
+    for k in range(4):
+        cfg.inlet_primitive[k] = float(inlet[k])
+    cfg.controller = _lib.CONTROLLERS[controller]
+    cfg.variant = _lib.VARIANTS[variant]
+    cfg.wavespeed = _lib.WAVESPEEDS[wavespeed]
+    return cfg
+
+
+def _dtype(precision):
+    if precision not in ("fp64", "fp32"):
+        raise ValueError("precision must be 'fp64' or 'fp32'")
+    return torch.float64 if precision == "fp64" else torch.float32
+
+
+class _Engine:
+    """One batch handle with its device memory (ring buffers and workspace)."""
+
+    def __init__(self, dim, precision, cfgs, states, device, tile=None, stream=None):
+        lib = _lib.load()
+        self.lib = lib
+        self.dim = dim
+        self.n = len(cfgs)
+        self.precision = precision
+        self.dtype = _dtype(precision)
+        self.device = device
+        self.stream = stream or torch.cuda.current_stream(device)
+        arr = (_lib.Config * self.n)(*cfgs)
+        handle = C.c_void_p()
+        t = None
+        if tile is not None:
+            t = _lib.Tile(*tile)
+        _lib.check(lib.tfv_batch_create(dim, _lib.TFV_FP64 if precision == "fp64" else _lib.TFV_FP32,
+                                        self.n, arr, C.byref(t) if t is not None else None,
+                                        C.byref(handle)))
+        self.handle = handle
+        ws = C.c_size_t()
+        _lib.check(lib.tfv_batch_workspace_size(handle, C.byref(ws)))
+        nring = C.c_int32()
+        _lib.check(lib.tfv_batch_ring_size(handle, C.byref(nring)))
+        self.nring = nring.value
+        self.workspace = torch.empty(ws.value + 256, dtype=torch.uint8, device=device)
+        off = (-self.workspace.data_ptr()) % 256
+        self.ws_ptr = self.workspace.data_ptr() + off
+        self.rings = []
+        ptrs = []
+        with torch.cuda.stream(self.stream):
+            for s in states:
+                ring = [torch.as_tensor(s, dtype=self.dtype).to(device, non_blocking=False)]
+                ring[0] = ring[0].contiguous()
+                for _ in range(self.nring - 1):
+                    ring.append(torch.empty_like(ring[0]))
+                self.rings.append(ring)
+                ptrs.extend(r.data_ptr() for r in ring)
+        self.stream.synchronize()
+        parr = (C.c_void_p * len(ptrs))(*ptrs)
+        _lib.check(lib.tfv_batch_bind(handle, C.c_void_p(self.ws_ptr), parr, None, None,
+                                      _lib.stream_ptr(self.stream)))
+        self.reports = (_lib.Report * self.n)()
+        self.refresh()
+
+    def advance(self, nsteps):
+        _lib.check(self.lib.tfv_batch_advance(self.handle, int(nsteps)))
+
+    def profile(self, nsteps):
+        """Milliseconds (step kernel, fallback, finalize) summed over nsteps."""
+        out = [C.c_float(), C.c_float(), C.c_float()]
+        _lib.check(self.lib.tfv_batch_profile(self.handle, int(nsteps), *[C.byref(v) for v in out]))
+        return [v.value for v in out]
+
+    def use_graph(self, steps):
+        _lib.check(self.lib.tfv_batch_use_graph(self.handle, int(steps)))
+
+    def refresh(self):
+        _lib.check(self.lib.tfv_batch_report(self.handle, self.reports))
+        return self.reports
+
+    def integrals(self):
+        out = (C.c_double * (5 * self.n))()
+        _lib.check(self.lib.tfv_batch_integrals(self.handle, out))
+        return np.array(out[:]).reshape(self.n, 5)
+
+    def current(self, i=0):
+        return self.rings[i][self.reports[i].current]
+
+    def replan(self):
+        _lib.check(self.lib.tfv_batch_replan(self.handle))
+        self.refresh()
+
+    def replan_async(self):
+        """Recompute dt from the current buffers without waiting."""
+        _lib.check(self.lib.tfv_batch_replan(self.handle))
+
+    def set_flux_outputs(self, i, fx, fy, fz):
+        _lib.check(self.lib.tfv_batch_set_flux_outputs(self.handle, i, _lib.ptr(fx), _lib.ptr(fy),
+                                                       _lib.ptr(fz)))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.tfv_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Simulation:
+    """Cartesian simulation session resumable between steps, on one GPU."""
+
+    def __init__(self, primitive, lengths, *, t_end, cfl=0.4, gamma=1.4, boundaries=None,
+                 limiter="VanLeer", reactive=False, kinetic_model="arrhenius", lambda_init=None,
+                 beta_init=None, inlet_primitive=None, controller="Sound Speed Controlled",
+                 variant="Variante 1 - Original", wavespeed="Pressure Based", max_steps=100000,
+                 geometry="cartesian", origins=None, face_boundaries=None, workers=1,
+                 precision="fp64", device=None, strict_cfl=True, chemistry=None, tile=None,
+                 graph_steps=0):
+        primitive = np.array(primitive, dtype=float, copy=True)
+        dim = primitive.ndim - 1
+        if dim not in (1, 2, 3) or primitive.shape[0] != dim + 2:
+            raise ValueError("Require primitives with shape (dimension+2, ... reversed spatial axes)")
+        lengths = list(np.atleast_1d(lengths))
+        counts = list(primitive.shape[1:][::-1])
+        if len(lengths) != dim:
+            raise ValueError("Lengths must be in x,y,z order, one per active axis")
+        boundaries = list(boundaries) if boundaries is not None else ["Open"] * dim
+        if geometry != "cartesian" or face_boundaries is not None:
+            raise NotImplementedError(
+                "metric/face-boundary sessions run on the reference's CPU kernel")
+        chem = dict(chemistry or {})
+        closure = chem.pop("closure", "si")
+        if closure not in _lib.CLOSURES:
+            raise ValueError("Unknown chemistry closure")
+        self.config = dict(
+            dimension=dim, counts_xyz=counts, lengths_xyz=lengths, boundaries_xyz=boundaries,
+            t_end=t_end, cfl=cfl, gamma=gamma, limiter=limiter, reactive=bool(reactive),
+            kinetic_model=kinetic_model,
+            inlet_primitive=list(DEFAULT_INLET if inlet_primitive is None else inlet_primitive),
+            controller=controller, variant=variant, wavespeed=wavespeed, max_steps=max_steps,
+            geometry=geometry, origins_xyz=(list(np.atleast_1d(origins)) if origins is not None
+                                            else [0.0] * dim))
+        self._strict_cfl = strict_cfl
+        self._closure = closure
+        self._chem = chem
+        self._validate_config()
+        if not np.isfinite(primitive).all() or np.any(primitive[[0, -1]] <= 0):
+            raise ValueError("Initial density and pressure must be positive and primitives finite")
+        if reactive:
+            raise NotImplementedError("reactive sessions are not available in this build yet")
+        if lambda_init is not None or beta_init is not None:
+            raise ValueError("Composition requires reactive chemistry; beta requires ZND")
+        if dim == 1:
+            raise NotImplementedError("1D sessions are not available in this build yet")
+        self.lam = None
+        self.beta = None
+        g = self.gamma
+        state = prim_to_cons(primitive, g)
+        if not _physical(state):
+            raise ValueError("Nonphysical initial conservative state")
+        self.precision = precision
+        self.device = torch.device(device) if device is not None else torch.device(
+            "cuda", torch.cuda.current_device())
+        cfg = make_config(dim, counts, lengths, boundaries, t_end=t_end, cfl=cfl, gamma=gamma,
+                          limiter=limiter, max_steps=max_steps, reactive=reactive,
+                          kinetic_model=kinetic_model, closure=closure, chemistry=chem,
+                          inlet_primitive=inlet_primitive, controller=controller,
+                          variant=variant, wavespeed=wavespeed)
+        self._engine = _Engine(dim, precision, [cfg], [state], self.device, tile=tile)
+        if graph_steps:
+            self._engine.use_graph(graph_steps)
+        self.run_id = str(uuid.uuid4())
+        self._workers = 1
+        self.set_workers(workers)
+
+    # -- validation (torchSession.py:190-254) -------------------------------
+    def _validate_config(self):
+        c = self.config
+        dim = c["dimension"]
+        for key in ("counts_xyz", "lengths_xyz", "boundaries_xyz"):
+            if len(c[key]) != dim:
+                raise ValueError("Incomplete mesh/boundary metadata")
+        for length, n in zip(c["lengths_xyz"], c["counts_xyz"]):
+            _validate_grid(length, n, c["cfl"], c["t_end"], self._strict_cfl)
+        if not np.isfinite(c["gamma"]) or c["gamma"] <= 1:
+            raise ValueError("gamma must be finite and greater than one")
+        if c["limiter"] not in LIMITERS or c["kinetic_model"] not in ("arrhenius", "znd"):
+            raise ValueError("Unknown limiter or chemistry model")
+        if (not isinstance(c["max_steps"], (int, np.integer)) or isinstance(c["max_steps"], bool)
+                or c["max_steps"] < 1):
+            raise ValueError("Invalid maximum steps")
+        for axis, boundary in enumerate(c["boundaries_xyz"]):
+            if boundary not in ("Open", "Reflective", "Periodic") and not (
+                    dim == 2 and axis == 1 and boundary == "Inflow"):
+                raise ValueError("Unsupported session boundary")
+        if c["controller"] not in _lib.CONTROLLERS or c["variant"] not in _lib.VARIANTS or \
+                c["wavespeed"] not in _lib.WAVESPEEDS:
+            raise ValueError("Unknown solver option")
+        if dim == 2 and "Inflow" in c["boundaries_xyz"]:
+            inlet = np.asarray(c["inlet_primitive"])
+            if (inlet.shape != (4,) or not np.isfinite(inlet).all() or inlet[0] <= 0
+                    or inlet[3] <= 0 or inlet[2] < 0):
+                raise ValueError("Invalid inlet primitives")
+
+    # -- workers: the GPU replaces the CPU flux pool (torchExecution.py) ----
+    @property
+    def workers(self):
+        return self._workers
+
+    def set_workers(self, workers):
+        if not isinstance(workers, int) or isinstance(workers, bool) or not 1 <= workers <= 64:
+            raise ValueError("Workers must be an integer from 1 to 64")
+        self._workers = workers
+        return self
+
+    def close(self):
+        pass
+
+    # -- state access --------------------------------------------------------
+    @property
+    def _report(self):
+        return self._engine.reports[0]
+
+    @property
+    def state(self):
+        return self._engine.current().detach().to("cpu", torch.float64).numpy()
+
+    @state.setter
+    def state(self, value):
+        value = np.asarray(value, dtype=float)
+        cur = self._engine.current()
+        if value.shape != tuple(cur.shape):
+            raise ValueError("state shape mismatch")
+        cur.copy_(torch.as_tensor(value, dtype=cur.dtype))
+        self._engine.replan()
+
+    @property
+    def device_state(self):
+        """The current state buffer on the GPU (no copy)."""
+        return self._engine.current()
+
+    @property
+    def time(self):
+        return self._report.time
+
+    @property
+    def steps(self):
+        return self._report.steps
+
+    @property
+    def dt(self):
+        return self._report.dt
+
+    @property
+    def initial_integral(self):
+        return np.array(self._report.initial_integral[:self.config["dimension"] + 2])
+
+    @property
+    def boundary_integral(self):
+        return np.array(self._report.boundary_integral[:self.config["dimension"] + 2])
+
+    @property
+    def source_integral(self):
+        return np.array(self._report.source_integral[:self.config["dimension"] + 2])
+
+    @property
+    def fallback_steps(self):
+        return self._report.fallback_steps
+
+    @property
+    def gamma(self):
+        if self.config["reactive"] and self._closure == "si" and self.lam is not None:
+            return (4.5 - self.lam) / (3.5 - self.lam)
+        return self.config["gamma"]
+
+    @property
+    def spacing(self):
+        return np.array(self.config["lengths_xyz"]) / self.config["counts_xyz"]
+
+    @property
+    def integral(self):
+        return self._engine.integrals()[0, :self.config["dimension"] + 2]
+
+    @property
+    def uses_metric_kernel(self):
+        return False
+
+    @property
+    def primitive(self):
+        s = self.state
+        p = s.copy()
+        p[1:-1] /= s[0]
+        p[-1] = (self.gamma - 1) * (s[-1] - 0.5 * np.sum(s[1:-1] ** 2, axis=0) / s[0])
+        return p
+
+    @property
+    def balance_residual(self):
+        return (self.integral - self.initial_integral + self.boundary_integral
+                - self.source_integral)
+
+    @property
+    def completed(self):
+        return self.time == self.config["t_end"]
+
+    # -- stepping ------------------------------------------------------------
+    def _raise_pending(self):
+        status = self._report.status
+        if status in (_lib.READY, _lib.DONE):
+            return
+        raise RuntimeError(_lib.STATUS_MESSAGES.get(status, _lib.STATUS[status]))
+
+    def step(self):
+        """Advance one complete split step; failed steps leave session data intact."""
+        if self.completed:
+            return
+        self._raise_pending()  # max steps / stall found when this step was planned
+        before = self.steps
+        self._engine.advance(1)
+        self._engine.refresh()
+        if self.steps == before:
+            self._raise_pending()  # the step itself failed; nothing was committed
+
+    def advance(self, nsteps):
+        """Enqueue ``nsteps`` steps without waiting (stops at t_end or on error)."""
+        self._engine.advance(nsteps)
+
+    def synchronize(self):
+        self._engine.refresh()
+        self._raise_pending()
+
+    def run(self, *, step_limit=None, checkpoint=None, checkpoint_every=0, output_prefix=None,
+            output_every=1, formats=("vtk", "xdmf"), chunk=64):
+        for value in (step_limit, checkpoint_every, output_every):
+            if value is not None and (not isinstance(value, int) or value < 0):
+                raise ValueError("Step intervals must be nonnegative integers")
+        if checkpoint or output_prefix:
+            raise NotImplementedError("checkpoint and field output need the reference's torchIO")
+        remaining = step_limit
+        while not self.completed and (remaining is None or remaining > 0):
+            self._raise_pending()
+            k = chunk if remaining is None else min(chunk, remaining)
+            before = self.steps
+            self._engine.advance(k)
+            self._engine.refresh()
+            if remaining is not None:
+                remaining -= self.steps - before
+            self._raise_pending()
+        return self
