@@ -214,6 +214,7 @@ def main():
         stop.record(stream)
         barrier()
     ms = start.elapsed_time(stop) / args.steps
+    eng.refresh()
     steps_done = sim.steps
     if dist is not None:
         t = torch.tensor([ms], device="cuda")
@@ -228,6 +229,7 @@ def main():
     achieved = BYTES_PER_CELL["fp32"] * cells / (step_kernel_ms * 1e-3) / 1e9
 
     # end to end: host state in pinned memory, H2D + step + D2H every step
+    eng.refresh()
     cur = eng.current()
     host_in = torch.empty(cur.shape, dtype=cur.dtype, pin_memory=True)
     host_out = torch.empty_like(host_in, pin_memory=True)

@@ -99,7 +99,8 @@ class _Engine:
         self.precision = precision
         self.dtype = _dtype(precision)
         self.device = device
-        self.stream = stream or torch.cuda.current_stream(device)
+        # a dedicated stream: graph capture is not allowed on the legacy default stream
+        self.stream = stream or torch.cuda.Stream(device)
         arr = (_lib.Config * self.n)(*cfgs)
         handle = C.c_void_p()
         t = None
@@ -299,20 +300,23 @@ class Simulation:
 
     @property
     def state(self):
+        self._engine.stream.synchronize()
         return self._engine.current().detach().to("cpu", torch.float64).numpy()
 
     @state.setter
     def state(self, value):
-        value = np.asarray(value, dtype=float)
+        value = np.array(value, dtype=float)
         cur = self._engine.current()
         if value.shape != tuple(cur.shape):
             raise ValueError("state shape mismatch")
-        cur.copy_(torch.as_tensor(value, dtype=cur.dtype))
+        with torch.cuda.stream(self._engine.stream):
+            cur.copy_(torch.as_tensor(value, dtype=cur.dtype))
         self._engine.replan()
 
     @property
     def device_state(self):
-        """The current state buffer on the GPU (no copy)."""
+        """The current state buffer on the GPU (no copy), ready to read."""
+        self._engine.stream.synchronize()
         return self._engine.current()
 
     @property

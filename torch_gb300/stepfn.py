@@ -28,7 +28,7 @@ def _device():
 
 
 def _as_device(x, dtype, device):
-    return torch.as_tensor(np.ascontiguousarray(x) if isinstance(x, np.ndarray) else x,
+    return torch.as_tensor(np.array(x, copy=True) if isinstance(x, np.ndarray) else x,
                            dtype=dtype, device=device).contiguous()
 
 
