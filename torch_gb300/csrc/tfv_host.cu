@@ -47,6 +47,7 @@ struct tfv_batch {
   std::vector<tfv_config> cfg;
   tfv_tile tile{};
   bool varg = false;
+  bool own_gamma = false;  // the per-cell gamma buffer lives in the workspace
   bool reactive = false;
   int nring = 2;
   std::vector<InstDesc> desc;
@@ -184,7 +185,7 @@ void layout(tfv_batch* b) {
   o = align_up(o + sizeof(double) * 5 * b->n, 256);
   b->off_gam = o;
   b->gam_bytes = 0;
-  if (b->varg) {
+  if (b->varg && b->own_gamma) {
     for (int i = 0; i < b->n; ++i) b->gam_bytes += align_up(real_size(b->precision) * b->desc[i].ncell, 256);
   }
   o += b->gam_bytes;
