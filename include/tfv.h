@@ -204,6 +204,27 @@ int tfv_hydro_step(const tfv_config* cfg, int32_t precision, const void* state_i
                    void* state_out, const void* gamma_cells, double dt, void* fx, void* fy,
                    void* fz, void* workspace, int32_t* used_fallback, void* stream);
 
+/* tfv_hydro_step without a workspace and without any device allocation.
+ * No counterpart in the reference (TORCH runs on the CPU and never touches
+ * device memory).  It is for callers that cannot call cudaMalloc: a host
+ * application that owns all GPU memory in a pool of its own and hands this
+ * library only the state and flux arrays, or a time-critical loop where the
+ * device-wide synchronisation an allocation implies is not acceptable.
+ * The step's scratch (descriptors, tile table, per-tile partial sums) lives
+ * in a 1 MiB array inside the library's device image; every GPU that loads
+ * the library holds it until the process exits.  Grids whose scratch would
+ * not fit are rejected with TFV_EINVAL (the limit is about 4,900 tiles: a
+ * 3D 256^3 grid needs 218 KiB in fp32 and 435 KiB in fp64).  The first call
+ * on a device looks the array's address up (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  Every
+ * call reuses the same array: a call rewrites the descriptors, tile table and
+ * scalars (the fallback flag starts at zero) and every partial sum before
+ * reading them, but calls that overlap on the GPU (other streams, other host
+ * threads) race on the array and must be serialised by the caller. */
+int tfv_hydro_step_static(const tfv_config* cfg, int32_t precision, const void* state_in,
+                          void* state_out, const void* gamma_cells, double dt, void* fx,
+                          void* fy, void* fz, int32_t* used_fallback, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -83,6 +83,8 @@ _SIGS = {
     "tfv_step_workspace_size": ([C.POINTER(Config), C.c_int32, C.POINTER(C.c_size_t)], C.c_int),
     "tfv_hydro_step": ([C.POINTER(Config), C.c_int32, _VP, _VP, _VP, C.c_double, _VP, _VP, _VP,
                         _VP, C.POINTER(C.c_int32), _VP], C.c_int),
+    "tfv_hydro_step_static": ([C.POINTER(Config), C.c_int32, _VP, _VP, _VP, C.c_double, _VP, _VP,
+                               _VP, C.POINTER(C.c_int32), _VP], C.c_int),
 }
 
 _lib = None

@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -544,3 +545,55 @@ int tfv_hydro_step(const tfv_config* cfg, int32_t precision, const void* state_i
 }
 
 }  // extern "C"
+
+// --------------------------------------------------------------------------
+// tfv_hydro_step_static: the stateless step with its scratch in a fixed array
+// of this library's device memory, for callers that cannot allocate.
+// --------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kStaticScratchBytes = size_t(1) << 20;  // 1 MiB on every device
+__device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+std::mutex g_static_mutex;
+constexpr int kMaxDevices = 256;
+void* g_static_ptr[kMaxDevices] = {};
+
+// Device address of g_static_scratch on the current device.  Host code may
+// not use the symbol itself (it names a host-side shadow); the address is
+// looked up once per device, with that device current.
+int static_scratch(void** out) {
+  int dev = 0;
+  TFV_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(TFV_EINVAL, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    TFV_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
+    if (!p) return fail(TFV_ECUDA, "cudaGetSymbolAddress returned a null address");
+    g_static_ptr[dev] = p;
+  }
+  *out = g_static_ptr[dev];
+  return TFV_OK;
+}
+
+}  // namespace
+
+extern "C" int tfv_hydro_step_static(const tfv_config* cfg, int32_t precision,
+                                     const void* state_in, void* state_out,
+                                     const void* gamma_cells, double dt, void* fx, void* fy,
+                                     void* fz, int32_t* used_fallback, void* stream) {
+  if (!cfg) return fail(TFV_EINVAL, "invalid arguments");
+  size_t need = 0;
+  int r = tfv_step_workspace_size(cfg, precision, &need);
+  if (r) return r;
+  if (need > kStaticScratchBytes)
+    return fail(TFV_EINVAL, "this grid needs " + std::to_string(need) +
+                                " bytes of step scratch but tfv_hydro_step_static holds " +
+                                std::to_string(kStaticScratchBytes) +
+                                "; use tfv_hydro_step with a workspace");
+  void* ws = nullptr;
+  r = static_scratch(&ws);
+  if (r) return r;
+  return tfv_hydro_step(cfg, precision, state_in, state_out, gamma_cells, dt, fx, fy, fz, ws,
+                        used_fallback, stream);
+}
