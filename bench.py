@@ -170,6 +170,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--tile", default=None, help="tx,ty,chunk[,persistent_ctas] of the FP32 step")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -192,7 +193,11 @@ def main():
     prim = explosion_3d(n)
     kw = dict(t_end=1e9, cfl=0.6, limiter="Superbee", boundaries=["Reflective"] * 3,
               strict_cfl=False, max_steps=10 ** 9)
-    sim = torch_gb300.Simulation(prim, [1, 1, 1], precision="fp32", graph_steps=1, **kw)
+    tile = None
+    if args.tile:
+        vals = [int(v) for v in args.tile.split(",")]
+        tile = tuple((vals + [0, 1][len(vals) - 3:])[:5]) if len(vals) < 5 else tuple(vals[:5])
+    sim = torch_gb300.Simulation(prim, [1, 1, 1], precision="fp32", graph_steps=1, tile=tile, **kw)
     eng = sim._engine
     stream = eng.stream
     cells = n ** 3
@@ -300,7 +305,8 @@ def main():
             "config": {"workload": "3D spherical explosion 256^3 FP32, Superbee, reflective, "
                                    "CFL 0.6", "grid": [n, n, n], "precision": "fp32 bulk, fp64 "
                                    "time and sums", "l2": "state 335 MB > L2, no flush",
-                       "parallelism": "replicas" if world > 1 else "single"},
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "tile": list(tile) if tile else "default"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
                          "kernel": "hydro_kernel<float,3>", "kernel_ms": step_kernel_ms,

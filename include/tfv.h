@@ -104,6 +104,8 @@ typedef struct tfv_tile {
   int32_t ty;      /* cells along y per tile (3D only; 1 otherwise) */
   int32_t chunk;   /* planes marched per tile (z in 3D, y in 2D) */
   int32_t persistent_ctas; /* 0 = one CTA per tile, else grid size of a persistent launch */
+  int32_t tma;     /* 1: stage planes with tensor copies (cp.async.bulk.tensor) where the
+                      grid allows it (x extent a multiple of 16 bytes); 0: plain loads */
 } tfv_tile;
 
 /* Per-instance scalars read back after steps. */

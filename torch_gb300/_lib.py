@@ -49,7 +49,7 @@ class Config(C.Structure):
 
 class Tile(C.Structure):
     _fields_ = [("tx", C.c_int32), ("ty", C.c_int32), ("chunk", C.c_int32),
-                ("persistent_ctas", C.c_int32)]
+                ("persistent_ctas", C.c_int32), ("tma", C.c_int32)]
 
 
 class Report(C.Structure):

@@ -2,6 +2,8 @@
 // division/square root allowed by the build flags; conservation sums and time
 // stay in double).
 #define REAL float
+// 80 registers: three 256-thread CTAs per SM (24 warps) without spills
+#define TFV_HYDRO_MIN_BLOCKS 3
 #define TFV_LAUNCH_NAME launch_step_f32
 #define TFV_SMEM_NAME hydro_smem_f32
 #define TFV_HLLC_NAME launch_hllc_f32

@@ -1,6 +1,8 @@
 // Double-precision step kernels: the reference-faithful path.  Built with
 // -fmad=false so every product and sum rounds separately, as in NumPy.
 #define REAL double
+// double precision needs ~250 registers; one CTA bound, 128-thread tiles
+#define TFV_HYDRO_MIN_BLOCKS 1
 #define TFV_DEFINE_SHARED_KERNELS
 #define TFV_LAUNCH_NAME launch_step_f64
 #define TFV_SMEM_NAME hydro_smem_f64

@@ -2,6 +2,8 @@
 // workspace layout, step sequencing and CUDA-graph capture.  The library
 // never allocates device memory: the caller passes a workspace and the state
 // buffers.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -53,10 +55,15 @@ struct tfv_batch {
   int nring = 2;
   std::vector<InstDesc> desc;
   std::vector<Tile> tiles;
+  struct Group {
+    int limiter, t_begin, t_end;
+  };
+  std::vector<Group> groups;  // contiguous tile ranges sharing a limiter
   std::vector<InstState> st;
   // workspace layout (bytes)
   size_t off_desc = 0, off_st = 0, off_tiles = 0, off_bsum = 0, off_wmax = 0, off_sum = 0,
-         off_flags = 0, off_int = 0, off_gam = 0, total = 0;
+         off_flags = 0, off_int = 0, off_gam = 0, off_tmaps = 0, total = 0;
+  std::vector<CUtensorMap> tmaps;  // [n][4]: ring buffers 0..2, gamma
   size_t gam_bytes = 0;
   unsigned char* ws = nullptr;
   cudaStream_t stream = nullptr;
@@ -97,8 +104,14 @@ int validate(const tfv_config& c, int dim) {
 
 void build_tiles(tfv_batch* b) {
   b->tiles.clear();
+  b->groups.clear();
   const int tx = b->tile.tx, ty = b->dim == 3 ? b->tile.ty : 1, ch = b->tile.chunk;
-  for (int i = 0; i < b->n; ++i) {
+  // instances ordered by limiter so that each limiter's tiles are contiguous
+  std::vector<int> order(b->n);
+  for (int i = 0; i < b->n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return b->cfg[x].limiter < b->cfg[y].limiter; });
+  for (int i : order) {
     const tfv_config& c = b->cfg[i];
     InstDesc& d = b->desc[i];
     d.tile0 = (int)b->tiles.size();
@@ -117,6 +130,9 @@ void build_tiles(tfv_batch* b) {
           b->tiles.push_back(t);
         }
     d.ntiles = (int)b->tiles.size() - d.tile0;
+    if (b->groups.empty() || b->groups.back().limiter != c.limiter)
+      b->groups.push_back({c.limiter, d.tile0, d.tile0});
+    b->groups.back().t_end = (int)b->tiles.size();
   }
 }
 
@@ -184,6 +200,8 @@ void layout(tfv_batch* b) {
   o = align_up(o + sizeof(int32_t) * nt, 256);
   b->off_int = o;
   o = align_up(o + sizeof(double) * 5 * b->n, 256);
+  b->off_tmaps = o;
+  o = align_up(o + sizeof(CUtensorMap) * 4 * b->n, 256);
   b->off_gam = o;
   b->gam_bytes = 0;
   if (b->varg && b->own_gamma) {
@@ -193,13 +211,85 @@ void layout(tfv_batch* b) {
   b->total = align_up(o, 256);
 }
 
-cudaError_t launch(tfv_batch* b, int op, int src_off, int dst_off) {
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// Tensor map of one state buffer (scalar=false: dims x, y, [z], component)
+// or of the per-cell gamma buffer (scalar=true), with the box the step
+// kernel stages per plane: x from x0 - 16 bytes over tx + 32 bytes, y over
+// ty + 4 cells, one plane.  False when the grid does not allow tensor copies.
+bool encode_map(CUtensorMap* m, const tfv_batch* b, const InstDesc& d, void* base, bool scalar) {
+  auto fn = encode_fn();
+  if (!fn || !base) return false;
+  const int es = b->precision == TFV_FP64 ? 8 : 4;
+  const int xo = 16 / es;
+  const int tx = b->tile.tx, ty = b->dim == 3 ? b->tile.ty : 1;
+  if ((d.n[0] * es) % 16 != 0 || reinterpret_cast<uintptr_t>(base) % 16 != 0 || tx % xo != 0 ||
+      tx + 2 * xo > 256 || ty + 4 > 256)
+    return false;
+  const int nv = b->dim + 2;
+  cuuint64_t dims[4], strides[3];
+  cuuint32_t box[4], estr[4] = {1, 1, 1, 1};
+  cuuint32_t rank;
+  const cuuint64_t nx = d.n[0], ny = d.n[1], nz = d.n[2];
+  if (b->dim == 3) {
+    dims[0] = nx; dims[1] = ny; dims[2] = nz; dims[3] = nv;
+    strides[0] = nx * es; strides[1] = nx * ny * es; strides[2] = nx * ny * nz * es;
+    box[0] = tx + 2 * xo; box[1] = ty + 4; box[2] = 1; box[3] = nv;
+    rank = scalar ? 3 : 4;
+  } else {
+    dims[0] = nx; dims[1] = ny; dims[2] = nv;
+    strides[0] = nx * es; strides[1] = nx * ny * es;
+    box[0] = tx + 2 * xo; box[1] = 1; box[2] = nv;
+    rank = scalar ? 2 : 3;
+  }
+  const CUresult r = fn(m, es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                        rank, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+int grid_for(const tfv_batch* b, int ntiles) {
+  return b->tile.persistent_ctas > 0 ? std::min<int>(b->tile.persistent_ctas, ntiles) : ntiles;
+}
+
+cudaError_t launch_range(tfv_batch* b, int op, int lim, int t0, int t1, int src_off, int dst_off) {
+  if (t1 <= t0) return cudaSuccess;
   StepArgs A = b->args;
   A.src_off = src_off;
   A.dst_off = dst_off;
+  A.t_begin = t0;
+  A.t_end = t1;
+  const int grid = grid_for(b, t1 - t0);
   if (b->precision == TFV_FP64)
-    return launch_step_f64(op, b->dim, b->varg, A, b->grid, b->block, b->stream);
-  return launch_step_f32(op, b->dim, b->varg, A, b->grid, b->block, b->stream);
+    return launch_step_f64(op, b->dim, b->varg, lim, A, grid, b->block, b->stream);
+  return launch_step_f32(op, b->dim, b->varg, lim, A, grid, b->block, b->stream);
+}
+
+// The step kernel is instantiated per limiter: one launch per limiter group.
+cudaError_t launch(tfv_batch* b, int op, int src_off, int dst_off) {
+  if (op == kOpHydro) {
+    for (const auto& g : b->groups) {
+      cudaError_t e = launch_range(b, op, g.limiter, g.t_begin, g.t_end, src_off, dst_off);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+  return launch_range(b, op, 0, 0, (int)b->tiles.size(), src_off, dst_off);
 }
 
 cudaError_t finalize(tfv_batch* b, int mode, int dst_off) {
@@ -260,13 +350,27 @@ static int create_internal(int32_t dim, int32_t precision, int32_t n, const tfv_
   } else {
     b->tile.tx = dim == 3 ? 32 : 128;
     b->tile.ty = dim == 3 ? (precision == TFV_FP64 ? 4 : 8) : 1;
-    b->tile.chunk = dim == 3 ? 64 : 32;
+    b->tile.chunk = dim == 3 ? 32 : 32;
     b->tile.persistent_ctas = 0;
+    b->tile.tma = 1;
   }
   if (dim != 3) b->tile.ty = 1;
-  if (b->tile.tx < 4 || b->tile.ty < 1 || b->tile.chunk < 1 || b->tile.tx * b->tile.ty > 256) {
+  {
+    // per-thread work items of the step kernel: ring cells <= 3, faces <= 4
+    const int tx = b->tile.tx, ty = b->tile.ty, nt = tx * ty;
+    const int ring = dim == 3 ? 2 * tx + 2 * ty + 4 : 2;
+    const int faces = (tx + 1) * ty + (dim == 3 ? tx * (ty + 1) : 0);
+    if (ring > 3 * nt || faces > 4 * nt) {
+      delete b;
+      return fail(TFV_EINVAL, "tile shape leaves too much ring or face work per thread");
+    }
+  }
+  if (b->tile.tx < 4 || b->tile.ty < 1 || b->tile.chunk < 1 || b->tile.tx * b->tile.ty > 256 ||
+      (b->tile.tx * b->tile.ty) % 32 != 0) {
     delete b;
-    return fail(TFV_EINVAL, "tile shape must have tx >= 4, ty >= 1, chunk >= 1, tx*ty <= 256");
+    return fail(TFV_EINVAL,
+                "tile shape must have tx >= 4, ty >= 1, chunk >= 1, tx*ty a multiple of 32 "
+                "and at most 256");
   }
   b->varg = varg;
   b->nring = 2;
@@ -308,6 +412,14 @@ int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* con
     }
     d.has_flux_out = 0;
   }
+  b->tmaps.assign((size_t)b->n * 4, CUtensorMap{});
+  for (int i = 0; i < b->n; ++i) {
+    InstDesc& d = b->desc[i];
+    bool ok = b->tile.tma != 0;
+    for (int k = 0; k < b->nring && ok; ++k) ok = encode_map(&b->tmaps[i * 4 + k], b, d, d.U[k], false);
+    if (ok && b->varg) ok = encode_map(&b->tmaps[i * 4 + 3], b, d, d.gam, true);
+    d.tma = ok ? 1 : 0;
+  }
   for (int i = 0; i < b->n; ++i) {
     InstState& s = b->st[i];
     std::memset(&s, 0, sizeof(s));
@@ -325,15 +437,18 @@ int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* con
   A.t_wmax = reinterpret_cast<double*>(b->ws + b->off_wmax);
   A.t_sum = reinterpret_cast<double*>(b->ws + b->off_sum);
   A.t_flags = reinterpret_cast<int32_t*>(b->ws + b->off_flags);
+  A.tmaps = b->ws + b->off_tmaps;
   b->block = b->tile.tx * b->tile.ty;
-  b->grid = b->tile.persistent_ctas > 0 ? std::min<int>(b->tile.persistent_ctas, A.ntiles)
-                                        : A.ntiles;
+  b->grid = grid_for(b, A.ntiles);
   TFV_CUDA(cudaMemcpyAsync(b->ws + b->off_desc, b->desc.data(), sizeof(InstDesc) * b->n,
                            cudaMemcpyHostToDevice, b->stream));
   TFV_CUDA(cudaMemcpyAsync(b->ws + b->off_st, b->st.data(), sizeof(InstState) * b->n,
                            cudaMemcpyHostToDevice, b->stream));
   TFV_CUDA(cudaMemcpyAsync(b->ws + b->off_tiles, b->tiles.data(), sizeof(Tile) * b->tiles.size(),
                            cudaMemcpyHostToDevice, b->stream));
+  TFV_CUDA(cudaMemcpyAsync(b->ws + b->off_tmaps, b->tmaps.data(),
+                           sizeof(CUtensorMap) * b->tmaps.size(), cudaMemcpyHostToDevice,
+                           b->stream));
   // initial integrals and first dt
   TFV_CUDA(launch(b, kOpWaves, 0, 0));
   TFV_CUDA(finalize(b, 3, 0));
@@ -525,6 +640,10 @@ int tfv_hydro_step(const tfv_config* cfg, int32_t precision, const void* state_i
     // the step uses the caller's dt instead of the planned one
     InstState s = b->st[0];
     s.dt = dt;
+    for (int k = 0; k < 3; ++k) {
+      s.coef_half[k] = (0.5 * dt) / b->desc[0].h[k];
+      s.coef_full[k] = dt / b->desc[0].h[k];
+    }
     s.status = TFV_READY;
     cudaError_t e = cudaMemcpyAsync(b->ws + b->off_st, &s, sizeof(s), cudaMemcpyHostToDevice,
                                     b->stream);

@@ -33,7 +33,8 @@ namespace tfv {
 
 enum : int { kBcOpen = 0, kBcReflective = 1, kBcPeriodic = 2, kBcInflow = 3 };
 enum : int { kReady = 0, kDone = 1, kErrMaxSteps = 2, kErrStall = 3, kErrNonphysical = 4,
-             kErrReactive = 5, kErrSpecies = 6, kErrChemistry = 7, kRetry = 8 };
+             kErrReactive = 5, kErrSpecies = 6, kErrChemistry = 7, kRetry = 8,
+             kErrDeviceWait = 9 };
 
 // Source index of padded coordinate i on an axis of n >= 2 cells (at most two
 // cells outside), following np.pad 'edge' / 'symmetric' / 'wrap'
@@ -106,6 +107,74 @@ __device__ __forceinline__ int block_or(int v, int* scratch) {
   return t;
 }
 
+
+// --------------------------------------------------------------------------
+// Tensor-memory-accelerator staging (cp.async.bulk.tensor + mbarrier).
+// Every wait is bounded: after kWaitLimit polls the caller reports an error
+// instead of spinning forever.
+// --------------------------------------------------------------------------
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Bounded wait for the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const void* map, int x, int y, int z,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(void* dst, const void* map, int x, int y, int z,
+                                            int w, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // --------------------------------------------------------------------------
 // Geometry helper: the grid seen as planes along the marching axis.
 // 3D: (a, b, p) = (x, y, z); 2D: (a, b, p) = (x, -, y).
@@ -156,18 +225,28 @@ template <typename R, int DIM, bool VARG>
 struct HydroSmem {
   static constexpr int NV = DIM + 2;
   static constexpr int NL = NV + (VARG ? 1 : 0);
-  int tx, ty, pw, ph, bw, bh;
-  size_t ring_off, box_off, fa_off, fb_off, bs_off, red_off, bytes;
+  static constexpr int kMaxRingItems = 3;  // ring + corner cells per thread
+  static constexpr int kMaxFaceItems = 4;  // in-plane faces per thread
+  // x offset of cell a = 0 in a staged row: a tensor-copy box must start on a
+  // 16-byte boundary, so the row holds 16 bytes of halo on each side.
+  static constexpr int kXo = 16 / (int)sizeof(R);
+  int tx, ty, pw, ph, bw, bh, xo;
+  size_t slot_elems;  // elements per ring slot (128-byte multiple)
+  size_t ring_off, bar_off, box_off, fa_off, fb_off, bs_off, red_off, items_off, bytes;
   __host__ __device__ void init(int tx_, int ty_) {
     tx = tx_;
     ty = DIM == 3 ? ty_ : 1;
-    pw = tx + 4;
+    xo = kXo;
+    pw = tx + 2 * kXo;
     ph = DIM == 3 ? ty + 4 : 1;
     bw = tx + 2;
     bh = DIM == 3 ? ty + 2 : 1;
+    slot_elems = ((size_t)NL * ph * pw * sizeof(R) + 127) / 128 * 128 / sizeof(R);
     size_t o = 0;
-    ring_off = o;
-    o += sizeof(R) * 3 * NL * ph * pw;
+    ring_off = o;  // dynamic shared memory starts 128-byte aligned
+    o += sizeof(R) * 3 * slot_elems;
+    bar_off = o;   // one mbarrier per ring slot
+    o += 8 * 4;
     o = (o + 15) & ~size_t(15);
     box_off = o;
     o += sizeof(R) * (DIM == 3 ? 3 : 2) * NV * bh * bw;
@@ -182,7 +261,9 @@ struct HydroSmem {
     o += sizeof(double) * (2 * ty * NV + (DIM == 3 ? 2 * tx * NV : 0) + 2 * NV);
     red_off = o;  // reduction scratch
     o += sizeof(double) * 40;
-    bytes = (o + 15) & ~size_t(15);
+    items_off = o;  // per-thread ring and face work items, packed
+    o += sizeof(int) * (kMaxRingItems + kMaxFaceItems) * tx * ty;
+    bytes = ((o + 15) & ~size_t(15)) + 128;  // + room to align the base to 128 bytes
   }
 };
 
@@ -203,31 +284,66 @@ struct HydroTile {
     const bool inside_p = (p >= 0 && p < g.np);
     const bool inside_a = (x0 >= 2 && x0 + ax + 2 <= g.na);
     const bool inside_b = DIM == 2 || (y0 >= 2 && y0 + by + 2 <= g.nb);
-    const int n = NL * h * w;
+    // one warp per staged row (component c, in-plane row lb); lanes along x
+    const int nrows = NL * h;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
     if (inside_p && inside_a && inside_b) {
       const int64_t base = (int64_t)p * g.ps + (int64_t)(DIM == 3 ? y0 - 2 : 0) * g.na + (x0 - 2);
-      for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int c = e / (h * w);
-        const int r = e - c * (h * w);
-        const int lb = r / w;
-        const int la = r - lb * w;
-        const int64_t off = base + (int64_t)lb * g.na + la;
-        R v;
-        if (VARG && c == NV)
-          v = gam[off];
-        else
-          v = U[c * g.cs + off];
-        dst[c * plane + lb * S.pw + la] = v;
+      for (int row = threadIdx.x >> 5; row < nrows; row += nwarps) {
+        const int c = row / h;
+        const int lb = row - c * h;
+        const R* srow = (VARG && c == NV) ? gam + base + (int64_t)lb * g.na
+                                          : U + c * g.cs + base + (int64_t)lb * g.na;
+        R* drow = dst + c * plane + lb * S.pw + (S.xo - 2);
+        for (int la = lane; la < w; la += 32) drow[la] = srow[la];
       }
     } else {
-      for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int c = e / (h * w);
-        const int r = e - c * (h * w);
-        const int lb = r / w;
-        const int la = r - lb * w;
-        dst[c * plane + lb * S.pw + la] = fetch_padded<R, DIM>(
-            d, g, U, VARG ? gam : (const R*)nullptr, c, x0 - 2 + la, DIM == 3 ? y0 - 2 + lb : 0, p);
+      for (int row = threadIdx.x >> 5; row < nrows; row += nwarps) {
+        const int c = row / h;
+        const int lb = row - c * h;
+        R* drow = dst + c * plane + lb * S.pw + (S.xo - 2);
+        for (int la = lane; la < w; la += 32)
+          drow[la] = fetch_padded<R, DIM>(d, g, U, VARG ? gam : (const R*)nullptr, c, x0 - 2 + la,
+                                          DIM == 3 ? y0 - 2 + lb : 0, p);
       }
+    }
+  }
+
+  // After a tensor copy of an in-range plane: rewrite the in-plane ghost
+  // cells (outside the domain, zero-filled by the copy) by the boundary
+  // rules.  Only tiles touching an in-plane domain edge have any.
+  static __device__ __forceinline__ void fix_ghosts(const InstDesc& d, const Geo<DIM>& g,
+                                                    const R* U, const R* gam, R* dst,
+                                                    const HydroSmem<R, DIM, VARG>& S, int x0,
+                                                    int y0, int ax, int by, int p) {
+    const int H = DIM == 3 ? by + 4 : 1;
+    const int aL = x0 == 0 ? 2 : 0;
+    const int aR = max(0, x0 + ax + 2 - g.na);
+    const int bL = (DIM == 3 && y0 == 0) ? 2 : 0;
+    const int bR = DIM == 3 ? max(0, y0 + by + 2 - g.nb) : 0;
+    const int wm = ax + 4 - aL - aR;
+    const int n1 = (aL + aR) * H;  // ghost columns, every row
+    const int n2 = (bL + bR) * wm; // ghost rows, the other columns
+    const int n = n1 + n2;
+    if (n == 0) return;
+    const int cplane = S.ph * S.pw;
+    for (int e = threadIdx.x; e < NL * n; e += blockDim.x) {
+      const int c = e / n;
+      const int r = e - c * n;
+      int la, lb;  // needed-region coordinates: a = la - 2, b = lb - 2
+      if (r < n1) {
+        const int col = r / H;
+        lb = r - col * H;
+        la = col < aL ? col : (ax + 4 - aR) + (col - aL);
+      } else {
+        const int q = r - n1;
+        const int row = q / wm;
+        la = aL + (q - row * wm);
+        lb = row < bL ? row : (by + 4 - bR) + (row - bL);
+      }
+      dst[c * cplane + lb * S.pw + la + (S.xo - 2)] = fetch_padded<R, DIM>(
+          d, g, U, VARG ? gam : (const R*)nullptr, c, x0 - 2 + la, DIM == 3 ? y0 - 2 + lb : 0, p);
     }
   }
 };
@@ -237,14 +353,14 @@ struct HydroTile {
 // 135-151, python/cfdSolver/torchSolver2D.py:305-377).  Writes predictor and
 // in-plane slopes to the box; returns the marching-axis slope; sets *gate when
 // a predicted face state is nonphysical (3D gate, torchSolver3D.py:152-159).
-template <typename R, int DIM, bool VARG>
+template <typename R, int DIM, bool VARG, int LIM>
 __device__ __forceinline__ void cell_stage(const R* ringm, const R* ringc, const R* ringp,
                                            R* box, const HydroSmem<R, DIM, VARG>& S, int a,
-                                           int b, int limiter, R gconst, const R* coefh,
-                                           R* ubar, R* smarch, bool& gate) {
+                                           int b, R gconst, const R* coefh, R* ubar, R* smarch,
+                                           bool& gate) {
   constexpr int NV = DIM + 2;
   const int plane = S.ph * S.pw;
-  const int li = (DIM == 3 ? (b + 2) * S.pw : 0) + (a + 2);
+  const int li = (DIM == 3 ? (b + 2) * S.pw : 0) + (a + S.xo);
   const int bi = (DIM == 3 ? (b + 1) * S.bw : 0) + (a + 1);
   const int bplane = S.bh * S.bw;
   R* bub = box;                   // predictor
@@ -274,7 +390,7 @@ __device__ __forceinline__ void cell_stage(const R* ringm, const R* ringc, const
         um = ringc[c * plane + li - S.pw];
         up = ringc[c * plane + li + S.pw];
       }
-      s[c] = limited_slope<R, DIM>(um, u[c], up, limiter);
+      s[c] = limited_slope<R, DIM, LIM>(um, u[c], up);
     }
     R vp[NV], vm[NV], fp[NV], fm[NV];
 #pragma unroll
@@ -338,10 +454,18 @@ __device__ __forceinline__ void wave_speeds(const R* u, R g, R* w) {
   if (DIM == 3) {
     const R rho = u[0];
     const R s = (u[1] * u[1] + u[2] * u[2]) + u[3] * u[3];
-    const R p = (g - R(1)) * (u[4] - (R(0.5) * s) / rho);
-    const R a = sqrt((g * p) / rho);
+    if constexpr (Exact<R>::value) {
+      const R p = (g - R(1)) * (u[4] - (R(0.5) * s) / rho);
+      const R a = sqrt((g * p) / rho);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) w[k] = fabs(u[k + 1] / rho) + a;
+      for (int k = 0; k < 3; ++k) w[k] = fabs(u[k + 1] / rho) + a;
+    } else {
+      const R irho = rcp(rho);
+      const R p = (g - R(1)) * (u[4] - R(0.5) * s * irho);
+      const R a = sqrt(g * p * irho);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) w[k] = fabs(u[k + 1] * irho) + a;
+    }
   } else {
     const R rho = np_max(u[0], R(kFloor));
     const R vx = u[1] / rho;
@@ -359,16 +483,18 @@ __device__ __forceinline__ T* smem_at(unsigned char* base, size_t off) {
 }
 
 // One tile of the fused second-order step.
-template <typename R, int DIM, bool VARG>
-__device__ void hydro_tile(const StepArgs& A, int t, unsigned char* smem,
-                           const HydroSmem<R, DIM, VARG>& S) {
+// Returns false when a bounded wait on a tensor copy gave up (the instance's
+// status is set to kErrDeviceWait and the kernel stops).
+template <typename R, int DIM, bool VARG, int LIM>
+__device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
+                           const HydroSmem<R, DIM, VARG>& S, uint32_t& bar_phase) {
   constexpr int NV = DIM + 2;
   constexpr int NL = NV + (VARG ? 1 : 0);
   constexpr int MD = DIM - 1;
   const Tile T = A.tiles[t];
   const InstDesc& d = A.desc[T.inst];
   InstState& st = A.st[T.inst];
-  if (st.status != kReady) return;  // uniform over the CTA
+  if (st.status != kReady) return true;  // uniform over the CTA
   Geo<DIM> g;
   g.init(d);
   const int src = (st.cur + A.src_off) % d.nring;
@@ -377,13 +503,13 @@ __device__ void hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   R* Un = (R*)d.U[dst];
   const R* gam = VARG ? (const R*)d.gam : nullptr;
   const double dt = st.dt;
-  const int limiter = d.limiter;
   const R gconst = R(d.gamma);
+  (void)dt;
   R coefh[DIM], cu[DIM];
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
-    coefh[k] = R((0.5 * dt) / d.h[k]);
-    cu[k] = R(dt / d.h[k]);
+    coefh[k] = R(st.coef_half[k]);  // (0.5*dt)/h_d, computed when dt was planned
+    cu[k] = R(st.coef_full[k]);     // dt/h_d
   }
   const int x0 = T.x0, y0 = T.y0, p0 = T.p0, p1 = T.p1;
   const int ax = min(S.tx, g.na - x0);
@@ -396,7 +522,7 @@ __device__ void hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   const bool at_x0 = (x0 == 0), at_x1 = (x0 + ax == g.na);
   const bool at_y0 = DIM == 3 && y0 == 0, at_y1 = DIM == 3 && (y0 + by == g.nb);
 
-  const int plane = NL * S.ph * S.pw;
+  const int plane = (int)S.slot_elems;
   const int cplane = S.ph * S.pw;
   const int bplane = S.bh * S.bw;
   R* ring = smem_at<R>(smem, S.ring_off);
@@ -413,11 +539,63 @@ __device__ void hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   const int fa_plane = S.ty * (S.tx + 1);
   const int fb_plane = (S.ty + 1) * S.tx;
 
-  auto slot = [&](int p) { return ring + ((p - p0 + 2) % 3) * plane; };
-  HydroTile<R, DIM, VARG>::load_plane(d, g, U, gam, slot(p0 - 2), S, x0, y0, ax, by, p0 - 2);
-  HydroTile<R, DIM, VARG>::load_plane(d, g, U, gam, slot(p0 - 1), S, x0, y0, ax, by, p0 - 1);
-  HydroTile<R, DIM, VARG>::load_plane(d, g, U, gam, slot(p0), S, x0, y0, ax, by, p0);
-  __syncthreads();
+  auto slot_of = [&](int p) { return (p - p0 + 2) % 3; };
+  auto slot = [&](int p) { return ring + slot_of(p) * plane; };
+  // Staging: an in-range plane of a tensor-copy-enabled instance arrives by
+  // one cp.async.bulk.tensor per plane (plus one for gamma); ghost planes
+  // and other instances use plain loads.
+  const bool use_tma = d.tma != 0;
+  const bool edge_tile = x0 == 0 || x0 + ax + 2 > g.na ||
+                         (DIM == 3 && (y0 == 0 || y0 + by + 2 > g.nb));
+  const char* maps = reinterpret_cast<const char*>(A.tmaps) + (size_t)T.inst * 4 * 128;
+  const void* map_u = maps + src * 128;
+  const void* map_g = maps + 3 * 128;
+  const uint32_t box_bytes = (uint32_t)(sizeof(R) * NV * S.ph * S.pw);
+  const uint32_t gbox_bytes = VARG ? (uint32_t)(sizeof(R) * S.ph * S.pw) : 0u;
+  uint64_t* bars = smem_at<uint64_t>(smem, S.bar_off);
+  bool waited_ok = true;
+  auto stage_begin = [&](int p) {
+    R* dst = slot(p);
+    if (use_tma && p >= 0 && p < g.np) {
+      if (tid == 0) {
+        uint64_t* bar = bars + slot_of(p);
+        fence_proxy_async();  // earlier generic accesses to the slot come first
+        mbar_expect_tx(bar, box_bytes + gbox_bytes);
+        if (DIM == 3) {
+          tma_load_4d(dst, map_u, x0 - S.xo, y0 - 2, p, 0, bar);
+          if (VARG) tma_load_3d(dst + NV * cplane, map_g, x0 - S.xo, y0 - 2, p, bar);
+        } else {
+          tma_load_3d(dst, map_u, x0 - S.xo, p, 0, bar);
+          if (VARG) tma_load_2d(dst + NV * cplane, map_g, x0 - S.xo, p, bar);
+        }
+      }
+    } else {
+      HydroTile<R, DIM, VARG>::load_plane(d, g, U, gam, dst, S, x0, y0, ax, by, p);
+    }
+  };
+  auto stage_end = [&](int p) {
+    if (use_tma && p >= 0 && p < g.np) {
+      const int sidx = slot_of(p);
+      const uint32_t parity = (bar_phase >> sidx) & 1u;
+      bar_phase ^= 1u << sidx;
+      if (!mbar_wait(bars + sidx, parity)) {
+        waited_ok = false;
+        mbar_wait(bars + sidx, parity);  // give the copy in flight a second bound
+      }
+      if (edge_tile)
+        HydroTile<R, DIM, VARG>::fix_ghosts(d, g, U, gam, slot(p), S, x0, y0, ax, by, p);
+    }
+  };
+  stage_begin(p0 - 2);
+  stage_begin(p0 - 1);
+  stage_begin(p0);
+  stage_end(p0 - 2);
+  stage_end(p0 - 1);
+  stage_end(p0);
+  if (__syncthreads_or(!waited_ok)) {
+    if (tid == 0) st.status = kErrDeviceWait;
+    return false;
+  }
 
   R Tprev[NV], Fprev[NV], Pprev[NV];
 #pragma unroll
@@ -440,45 +618,71 @@ __device__ void hydro_tile(const StepArgs& A, int t, unsigned char* smem,
     if (at_x1 && at_y1) { corner_a[ncorner] = ax; corner_b[ncorner++] = by; }
   }
 
+  // Per-thread work items, computed once per tile and kept in shared memory:
+  // ring/corner cells of the cross region and in-plane faces, packed as
+  // (kind << 30) | ((i + 1) << 15) | (j + 1).
+  int* items = smem_at<int>(smem, S.items_off);
+  const int NT = blockDim.x;
+  constexpr int MR = HydroSmem<R, DIM, VARG>::kMaxRingItems;
+  const int nring_cells = DIM == 3 ? 2 * ax + 2 * by : 2;
+  int n_ritems = 0;
+  for (int q = tid; q < nring_cells + ncorner; q += NT) {
+    int a, b;
+    if (q < nring_cells) {
+      if (DIM == 3) {
+        if (q < by) { a = -1; b = q; }
+        else if (q < 2 * by) { a = ax; b = q - by; }
+        else if (q < 2 * by + ax) { a = q - 2 * by; b = -1; }
+        else { a = q - 2 * by - ax; b = by; }
+      } else {
+        a = q == 0 ? -1 : ax;
+        b = 0;
+      }
+    } else {
+      a = corner_a[q - nring_cells];
+      b = corner_b[q - nring_cells];
+    }
+    items[n_ritems * NT + tid] = ((a + 1) << 15) | (b + 1);
+    ++n_ritems;
+  }
+  const int nfa = (ax + 1) * by;
+  const int nfb = DIM == 3 ? ax * (by + 1) : 0;
+  int n_fitems = 0;
+  for (int w = tid; w < nfa + nfb; w += NT) {
+    int packed;
+    if (w < nfa) {
+      const int af = w % (ax + 1), b = w / (ax + 1);
+      packed = ((af + 1) << 15) | (b + 1);
+    } else {
+      const int q = w - nfa;
+      const int a = q % ax, bf = q / ax;
+      packed = (1 << 30) | ((a + 1) << 15) | (bf + 1);
+    }
+    items[(MR + n_fitems) * NT + tid] = packed;
+    ++n_fitems;
+  }
+
   for (int it = p0 - 1; it <= p1; ++it) {
     const R* rm = slot(it - 1);
     const R* rc = slot(it);
     const R* rp = slot(it + 1);
     const bool full = (it >= p0 && it < p1);
     const bool edge_plane = DIM == 3 && (it == -1 || it == g.np);
-    int nring = 0, ncor = 0;
-    if (full || edge_plane) {
-      nring = DIM == 3 ? 2 * ax + 2 * by : 2;
-      ncor = ncorner;
-    }
-    const int ncell = nint + nring + ncor;
+    const int nr_now = (full || edge_plane) ? n_ritems : 0;
     R Bn[NV], Tn[NV];
 #pragma unroll
     for (int c = 0; c < NV; ++c) Bn[c] = Tn[c] = R(0);
-    for (int w = tid; w < ncell; w += blockDim.x) {
-      int a, b;
-      if (w < nint) {
-        a = w % ax;
-        b = w / ax;
-      } else if (w < nint + nring) {
-        const int q = w - nint;
-        if (DIM == 3) {
-          if (q < by) { a = -1; b = q; }
-          else if (q < 2 * by) { a = ax; b = q - by; }
-          else if (q < 2 * by + ax) { a = q - 2 * by; b = -1; }
-          else { a = q - 2 * by - ax; b = by; }
-        } else {
-          a = q == 0 ? -1 : ax;
-          b = 0;
-        }
-      } else {
-        const int q = w - nint - nring;
-        a = corner_a[q];
-        b = corner_b[q];
+    // k = -1: the owned interior cell; k >= 0: ring / corner cells
+    for (int k = owner ? -1 : 0; k < nr_now; ++k) {
+      int a = oa, b = ob;
+      if (k >= 0) {
+        const int pk = items[k * NT + tid];
+        a = ((pk >> 15) & 0x7fff) - 1;
+        b = (pk & 0x7fff) - 1;
       }
       R ub[NV], sm[NV];
-      cell_stage<R, DIM, VARG>(rm, rc, rp, box, S, a, b, limiter, gconst, coefh, ub, sm, gate);
-      if (w < nint) {
+      cell_stage<R, DIM, VARG, LIM>(rm, rc, rp, box, S, a, b, gconst, coefh, ub, sm, gate);
+      if (k < 0) {
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
           Bn[c] = ub[c] - R(0.5) * sm[c];
@@ -487,31 +691,40 @@ __device__ void hydro_tile(const StepArgs& A, int t, unsigned char* smem,
       }
     }
     __syncthreads();  // box complete; ring slot of plane it-1 free
-    if (it + 2 <= p1 + 1)
-      HydroTile<R, DIM, VARG>::load_plane(d, g, U, gam, slot(it + 2), S, x0, y0, ax, by, it + 2);
+    const bool stage_next = it + 2 <= p1 + 1;
+    if (stage_next) stage_begin(it + 2);
     if (full) {
-      const int nfa = (ax + 1) * by;
-      const int nfb = DIM == 3 ? ax * (by + 1) : 0;
       const R* bub = box;
-      const R* bsa = box + NV * bplane;
-      const R* bsb = box + 2 * NV * bplane;
-      for (int w = tid; w < nfa + nfb; w += blockDim.x) {
-        R L[NV], Rr[NV], F[NV];
-        R gl = gconst, gr = gconst;
-        if (w < nfa) {
-          const int af = w % (ax + 1), b = w / (ax + 1);
-          const int bl = (DIM == 3 ? (b + 1) * S.bw : 0) + af;  // box index of cell af-1
+      for (int k = 0; k < n_fitems; ++k) {
+        const int pk = items[(MR + k) * NT + tid];
+        const int kind = pk >> 30;  // 0: face normal to x, 1: normal to y (3D)
+        const int i = ((pk >> 15) & 0x7fff) - 1;
+        const int j = (pk & 0x7fff) - 1;
+        // left cell's box index, step to the right cell, slope array
+        const int bl = kind == 0 ? (DIM == 3 ? (j + 1) * S.bw : 0) + i : j * S.bw + i + 1;
+        const int br = bl + (kind == 0 ? 1 : S.bw);
+        const R* bsl = box + (kind == 0 ? 1 : 2) * NV * bplane;
+        // rotation into the normal basis: swap rows 1 and 2 for y faces
+        R ul[NV], ur[NV], f[NV];
 #pragma unroll
-          for (int c = 0; c < NV; ++c) {
-            L[c] = bub[c * bplane + bl] + R(0.5) * bsa[c * bplane + bl];
-            Rr[c] = bub[c * bplane + bl + 1] - R(0.5) * bsa[c * bplane + bl + 1];
-          }
-          if (VARG) {
-            const int li = (DIM == 3 ? (b + 2) * S.pw : 0) + af + 1;
-            gl = rc[NV * cplane + li];
-            gr = rc[NV * cplane + li + 1];
-          }
-          hllc_cartesian<R, NV>(L, Rr, gl, gr, 0, F);
+        for (int c = 0; c < NV; ++c) {
+          const int cc = (kind == 1 && c == 1) ? 2 : ((kind == 1 && c == 2) ? 1 : c);
+          ul[c] = bub[cc * bplane + bl] + R(0.5) * bsl[cc * bplane + bl];
+          ur[c] = bub[cc * bplane + br] - R(0.5) * bsl[cc * bplane + br];
+        }
+        R gl = gconst, gr = gconst;
+        if (VARG) {
+          const int li = kind == 0 ? (DIM == 3 ? (j + 2) * S.pw : 0) + i - 1 + S.xo
+                                   : (j + 1) * S.pw + i + S.xo;
+          gl = rc[NV * cplane + li];
+          gr = rc[NV * cplane + li + (kind == 0 ? 1 : S.pw)];
+        }
+        hllc<R, NV - 3>(ul, ur, gl, gr, f);
+        R F[NV];  // back to Cartesian order
+#pragma unroll
+        for (int c = 0; c < NV; ++c) F[c] = kind == 1 ? (c == 1 ? f[2] : (c == 2 ? f[1] : f[c])) : f[c];
+        if (kind == 0) {
+          const int af = i, b = j;
 #pragma unroll
           for (int c = 0; c < NV; ++c) fa[c * fa_plane + b * (S.tx + 1) + af] = F[c];
           if (af == 0 && at_x0) {
@@ -529,20 +742,7 @@ __device__ void hydro_tile(const StepArgs& A, int t, unsigned char* smem,
               fout[0][((int64_t)(c * g.np + it) * g.nb + (y0 + b)) * nf + x0 + af] = F[c];
           }
         } else {
-          const int q = w - nfa;
-          const int a = q % ax, bf = q / ax;
-          const int bl = bf * S.bw + a + 1;  // box index of cell (a, bf-1)
-#pragma unroll
-          for (int c = 0; c < NV; ++c) {
-            L[c] = bub[c * bplane + bl] + R(0.5) * bsb[c * bplane + bl];
-            Rr[c] = bub[c * bplane + bl + S.bw] - R(0.5) * bsb[c * bplane + bl + S.bw];
-          }
-          if (VARG) {
-            const int li = (bf + 1) * S.pw + a + 2;
-            gl = rc[NV * cplane + li];
-            gr = rc[NV * cplane + li + S.pw];
-          }
-          hllc_cartesian<R, NV>(L, Rr, gl, gr, 1, F);
+          const int a = i, bf = j;
 #pragma unroll
           for (int c = 0; c < NV; ++c) fb[c * fb_plane + bf * S.tx + a] = F[c];
           if (bf == 0 && at_y0) {
@@ -561,12 +761,16 @@ __device__ void hydro_tile(const StepArgs& A, int t, unsigned char* smem,
         }
       }
     }
-    __syncthreads();  // in-plane fluxes complete; plane it+2 staged
+    if (stage_next) stage_end(it + 2);
+    if (__syncthreads_or(!waited_ok)) {  // in-plane fluxes complete; plane it+2 staged
+      if (tid == 0) st.status = kErrDeviceWait;
+      return false;
+    }
     R Fm[NV];
 #pragma unroll
     for (int c = 0; c < NV; ++c) Fm[c] = R(0);
     if (owner) {
-      const int li = (DIM == 3 ? (ob + 2) * S.pw : 0) + oa + 2;
+      const int li = (DIM == 3 ? (ob + 2) * S.pw : 0) + oa + S.xo;
       const R gcur = VARG ? rc[NV * cplane + li] : gconst;
       if (it >= p0) {
         hllc_cartesian<R, NV>(Tprev, Bn, gprev, gcur, MD, Fm);
@@ -642,14 +846,25 @@ __device__ void hydro_tile(const StepArgs& A, int t, unsigned char* smem,
     if (fl & (kFlagNonphysical | kFlagGate)) atomicOr(&st.fb_word, fl);
   }
   __syncthreads();
+  return true;
 }
 
-template <typename R, int DIM, bool VARG>
-__global__ void __launch_bounds__(256) hydro_kernel(StepArgs A) {
-  extern __shared__ __align__(16) unsigned char smem[];
+template <typename R, int DIM, bool VARG, int LIM>
+__global__ void __launch_bounds__(256, TFV_HYDRO_MIN_BLOCKS) hydro_kernel(StepArgs A) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
   HydroSmem<R, DIM, VARG> S;
   S.init(A.tx, A.ty);
-  for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) hydro_tile<R, DIM, VARG>(A, t, smem, S);
+  if (threadIdx.x == 0) {
+    uint64_t* bars = smem_at<uint64_t>(smem, S.bar_off);
+    for (int k = 0; k < 3; ++k) mbar_init(bars + k, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  uint32_t bar_phase = 0;  // parity of the next completion of each slot's barrier
+  for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x)
+    if (!hydro_tile<R, DIM, VARG, LIM>(A, t, smem, S, bar_phase)) break;
 }
 
 // --------------------------------------------------------------------------
@@ -710,7 +925,7 @@ template <typename R, int DIM, bool VARG>
 __global__ void __launch_bounds__(256) fallback_kernel(StepArgs A) {
   constexpr int NV = DIM + 2;
   __shared__ double red[40];
-  for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
+  for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
     const Tile T = A.tiles[t];
     const InstDesc& d = A.desc[T.inst];
     InstState& st = A.st[T.inst];
@@ -723,9 +938,10 @@ __global__ void __launch_bounds__(256) fallback_kernel(StepArgs A) {
     R* Un = (R*)d.U[dst];
     const R* gam = VARG ? (const R*)d.gam : nullptr;
     const double dt = st.dt;
+    (void)dt;
     R cu[DIM];
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) cu[k] = R(dt / d.h[k]);
+    for (int k = 0; k < DIM; ++k) cu[k] = R(st.coef_full[k]);
     const int ax = min(A.tx, g.na - T.x0);
     const int by = DIM == 3 ? min(A.ty, g.nb - T.y0) : 1;
     const bool owner = (int)threadIdx.x < ax * by;
@@ -829,7 +1045,7 @@ template <typename R, int DIM, bool VARG>
 __global__ void __launch_bounds__(256) waves_kernel(StepArgs A) {
   constexpr int NV = DIM + 2;
   __shared__ double red[40];
-  for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
+  for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
     const Tile T = A.tiles[t];
     const InstDesc& d = A.desc[T.inst];
     const InstState& st = A.st[T.inst];
@@ -923,6 +1139,10 @@ __device__ __forceinline__ void plan_next(const InstDesc& d, InstState& st, cons
   const double rem = d.t_end - st.time;
   if (rem < dt) dt = rem;
   st.dt = dt;
+  for (int k = 0; k < 3; ++k) {
+    st.coef_half[k] = (0.5 * dt) / d.h[k];
+    st.coef_full[k] = dt / d.h[k];
+  }
   if (!isfinite(dt) || dt <= 0.0 || st.time + dt == st.time) {
     st.status = kErrStall;
     return;

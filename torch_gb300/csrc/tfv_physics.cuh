@@ -1,12 +1,16 @@
 // Device physics of TORCH's Cartesian finite-volume step, templated on the
-// arithmetic type R (double: reference-faithful path; float: bulk FP32 path).
+// arithmetic type R.
 //
-// Every expression keeps the operation order of the NumPy reference so that
-// the double instantiation, compiled without FMA contraction (-fmad=false),
-// reproduces the reference bit for bit: `a * b * c` in Python is (a*b)*c,
-// sums of squares over the component axis are sequential, masks follow the
-// reference's precedence.  The float instantiation uses the same formulas
-// with contraction and fast division allowed by its compile flags.
+// double — the reference-faithful path.  Every expression keeps the operation
+//   order of the NumPy reference so that, compiled without FMA contraction
+//   (-fmad=false), it reproduces the reference bit for bit: `a * b * c` in
+//   Python is (a*b)*c, sums of squares over the component axis are
+//   sequential, numpy.maximum/minimum propagate NaN, masks follow the
+//   reference's precedence.
+// float — the bulk FP32 path.  Same formulas, rearranged for throughput:
+//   one reciprocal per density instead of one division per use, approximate
+//   division and square root (MUFU), NaN-propagating min/max in one
+//   instruction, a single finiteness test per state.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -17,11 +21,33 @@ namespace tfv {
 constexpr double kFloor = 1e-12;  // density / pressure floor
 constexpr double kGuard = 1e-14;  // division guard (limiters, HLLC)
 
+template <typename R>
+struct Exact {
+  static constexpr bool value = false;
+};
+template <>
+struct Exact<double> {
+  static constexpr bool value = true;
+};
+
 // numpy.maximum / numpy.minimum: NaN propagates, first operand wins ties.
-template <typename R>
-__device__ __forceinline__ R np_max(R a, R b) { return (a >= b || a != a) ? a : b; }
-template <typename R>
-__device__ __forceinline__ R np_min(R a, R b) { return (a <= b || a != a) ? a : b; }
+__device__ __forceinline__ double np_max(double a, double b) { return (a >= b || a != a) ? a : b; }
+__device__ __forceinline__ double np_min(double a, double b) { return (a <= b || a != a) ? a : b; }
+__device__ __forceinline__ float np_max(float a, float b) {
+  float r;
+  asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float np_min(float a, float b) {
+  float r;
+  asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+
+// a / b: IEEE division (double) or the approximate single-precision one.
+__device__ __forceinline__ double dv(double a, double b) { return a / b; }
+__device__ __forceinline__ float dv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ float rcp(float b) { return __fdividef(1.0f, b); }
 
 // np.where(abs(x) < g, g, x)
 template <typename R>
@@ -31,43 +57,35 @@ template <typename R>
 __device__ __forceinline__ bool finite_(R x) { return isfinite(x); }
 
 // --------------------------------------------------------------------------
-// Limiters.
+// Limiters (LIM: 0 VanLeer, 1 Albada, 2 MINBEE, 3 Superbee, 4 Unos).
 // 3D: python/cfdSolver/torchSolver3D.py:86-111.
 // 2D: python/cfdSolver/torchSolver2D.py:124-168 (VanLeer/Albada zero for
 //     r <= 0, Unos without the (1+2r)/3 bound).
 // --------------------------------------------------------------------------
-template <typename R, int DIM>
-__device__ __forceinline__ R limited_slope(R um, R uc, R up, int limiter) {
+template <typename R, int DIM, int LIM>
+__device__ __forceinline__ R limited_slope(R um, R uc, R up) {
   const R minus = uc - um;
   const R plus = up - uc;
-  const R r = minus / guarded(plus, R(kGuard));
+  const R r = dv(minus, guarded(plus, R(kGuard)));
   R phi;
-  switch (limiter) {
-    case 1: {  // Albada
-      const R pos = np_max(r, R(0));
-      phi = (pos * pos + pos) / (pos * pos + R(1));
-      if (DIM == 2 && !(r > R(0))) phi = R(0);
-      break;
-    }
-    case 2:  // MINBEE
-      phi = np_max(R(0), np_min(r, R(1)));
-      break;
-    case 3:  // Superbee
-      phi = np_max(R(0), np_max(np_min(R(2) * r, R(1)), np_min(r, R(2))));
-      break;
-    case 4:  // Unos
-      if (DIM == 3)
-        phi = np_max(R(0), np_min(np_min(np_min(R(2), R(2) * r), (R(2) + r) / R(3)),
-                                  (R(1) + R(2) * r) / R(3)));
-      else
-        phi = np_max(R(0), np_min(np_min(R(2), R(2) * r), (R(2) + r) / R(3)));
-      break;
-    default: {  // VanLeer
-      const R pos = np_max(r, R(0));
-      phi = (R(2) * pos) / (R(1) + pos);
-      if (DIM == 2 && !(r > R(0))) phi = R(0);
-      break;
-    }
+  if (LIM == 1) {  // Albada
+    const R pos = np_max(r, R(0));
+    phi = dv(pos * pos + pos, pos * pos + R(1));
+    if (DIM == 2 && !(r > R(0))) phi = R(0);
+  } else if (LIM == 2) {  // MINBEE
+    phi = np_max(R(0), np_min(r, R(1)));
+  } else if (LIM == 3) {  // Superbee
+    phi = np_max(R(0), np_max(np_min(R(2) * r, R(1)), np_min(r, R(2))));
+  } else if (LIM == 4) {  // Unos
+    if (DIM == 3)
+      phi = np_max(R(0), np_min(np_min(np_min(R(2), R(2) * r), dv(R(2) + r, R(3))),
+                                dv(R(1) + R(2) * r, R(3))));
+    else
+      phi = np_max(R(0), np_min(np_min(R(2), R(2) * r), dv(R(2) + r, R(3))));
+  } else {  // VanLeer
+    const R pos = np_max(r, R(0));
+    phi = dv(R(2) * pos, R(1) + pos);
+    if (DIM == 2 && !(r > R(0))) phi = R(0);
   }
   return phi * plus;
 }
@@ -81,10 +99,17 @@ __device__ __forceinline__ R limited_slope(R um, R uc, R up, int limiter) {
 // --------------------------------------------------------------------------
 template <typename R>
 __device__ __forceinline__ void flux3(const R* u, R g, int m, R* f) {
-  const R rho = u[0];
   const R ssum = (u[1] * u[1] + u[2] * u[2]) + u[3] * u[3];
-  const R p = (g - R(1)) * (u[4] - (R(0.5) * ssum) / rho);
-  const R vel = u[m] / rho;
+  R p, vel;
+  if constexpr (Exact<R>::value) {
+    const R rho = u[0];
+    p = (g - R(1)) * (u[4] - (R(0.5) * ssum) / rho);
+    vel = u[m] / rho;
+  } else {
+    const R irho = rcp(u[0]);
+    p = (g - R(1)) * (u[4] - R(0.5) * ssum * irho);
+    vel = u[m] * irho;
+  }
 #pragma unroll
   for (int c = 0; c < 4; ++c) f[c] = u[c] * vel;
   f[m] = f[m] + p;
@@ -94,8 +119,15 @@ __device__ __forceinline__ void flux3(const R* u, R g, int m, R* f) {
 template <typename R>
 __device__ __forceinline__ void flux2(const R* u, R g, int normal, R* f) {
   const R rho = np_max(u[0], R(kFloor));
-  const R vx = u[1] / rho;
-  const R vy = u[2] / rho;
+  R vx, vy;
+  if constexpr (Exact<R>::value) {
+    vx = u[1] / rho;
+    vy = u[2] / rho;
+  } else {
+    const R irho = rcp(rho);
+    vx = u[1] * irho;
+    vy = u[2] * irho;
+  }
   const R p = np_max((g - R(1)) * (u[3] - (R(0.5) * rho) * (vx * vx + vy * vy)), R(kFloor));
   if (normal == 0) {
     f[0] = rho * vx;
@@ -113,13 +145,21 @@ __device__ __forceinline__ void flux2(const R* u, R g, int normal, R* f) {
 // Physical-state test of one cell (python/cfdSolver/torchSolver.py:1038-1046).
 template <typename R, int NV>
 __device__ __forceinline__ bool physical_cell(const R* u) {
-  bool ok = true;
-#pragma unroll
-  for (int c = 0; c < NV; ++c) ok = ok && finite_(u[c]);
   R s = u[1] * u[1];
 #pragma unroll
   for (int c = 2; c < NV - 1; ++c) s = s + u[c] * u[c];
-  return ok && (u[0] > R(kFloor)) && (u[NV - 1] - (R(0.5) * s) / u[0] > R(kFloor));
+  if constexpr (Exact<R>::value) {
+    bool ok = true;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) ok = ok && finite_(u[c]);
+    return ok && (u[0] > R(kFloor)) && (u[NV - 1] - (R(0.5) * s) / u[0] > R(kFloor));
+  } else {
+    // one finiteness test: any NaN or infinity makes the sum non-finite
+    R all = u[0];
+#pragma unroll
+    for (int c = 1; c < NV; ++c) all = all + u[c];
+    return finite_(all) && (u[0] > R(kFloor)) && (u[NV - 1] - R(0.5) * s * rcp(u[0]) > R(kFloor));
+  }
 }
 
 // --------------------------------------------------------------------------
@@ -132,16 +172,22 @@ template <typename R, int NT>
 __device__ __forceinline__ void hllc(const R* ul, const R* ur, R gl, R gr, R* out) {
   constexpr int NV = NT + 3;
   constexpr int E = NV - 1;
+  constexpr bool X = Exact<R>::value;
   const R g = R(0.5) * (gl + gr);
   const R rl = np_max(ul[0], R(kFloor));
   const R rr = np_max(ur[0], R(kFloor));
-  const R unl = ul[1] / rl;
-  const R unr = ur[1] / rr;
+  R irl = R(0), irr = R(0);
+  if constexpr (!X) {
+    irl = rcp(rl);
+    irr = rcp(rr);
+  }
+  const R unl = X ? ul[1] / rl : ul[1] * irl;
+  const R unr = X ? ur[1] / rr : ur[1] * irr;
   R utl[NT], utr[NT];
 #pragma unroll
   for (int t = 0; t < NT; ++t) {
-    utl[t] = ul[2 + t] / rl;
-    utr[t] = ur[2 + t] / rr;
+    utl[t] = X ? ul[2 + t] / rl : ul[2 + t] * irl;
+    utr[t] = X ? ur[2 + t] / rr : ur[2 + t] * irr;
   }
   R stl = utl[0] * utl[0], str = utr[0] * utr[0];
 #pragma unroll
@@ -153,8 +199,8 @@ __device__ __forceinline__ void hllc(const R* ul, const R* ur, R gl, R gr, R* ou
   const R ker = (R(0.5) * rr) * (unr * unr + str);
   const R pl = np_max((gl - R(1)) * (ul[E] - kel), R(kFloor));
   const R pr = np_max((gr - R(1)) * (ur[E] - ker), R(kFloor));
-  const R al = sqrt((gl * pl) / rl);
-  const R ar = sqrt((gr * pr) / rr);
+  const R al = X ? sqrt((gl * pl) / rl) : sqrt(gl * pl * irl);
+  const R ar = X ? sqrt((gr * pr) / rr) : sqrt(gr * pr * irr);
 
   R fl[NV], fr[NV];
   fl[0] = rl * unl;
@@ -171,7 +217,7 @@ __device__ __forceinline__ void hllc(const R* ul, const R* ur, R gl, R gr, R* ou
 
   const R sql = sqrt(rl);
   const R sqr = sqrt(rr);
-  const R inv = R(1) / (sql + sqr);
+  const R inv = X ? R(1) / (sql + sqr) : rcp(sql + sqr);
   const R uroe = (sql * unl + sqr * unr) * inv;
   R vsum;
   {
@@ -183,8 +229,8 @@ __device__ __forceinline__ void hllc(const R* ul, const R* ur, R gl, R gr, R* ou
       vsum = vsum + vt * vt;
     }
   }
-  const R hl = (ul[E] + pl) / rl;
-  const R hr = (ur[E] + pr) / rr;
+  const R hl = X ? (ul[E] + pl) / rl : (ul[E] + pl) * irl;
+  const R hr = X ? (ur[E] + pr) / rr : (ur[E] + pr) * irr;
   const R hroe = (sql * hl + sqr * hr) * inv;
   const R keroe = R(0.5) * (uroe * uroe + vsum);
   const R aroe = sqrt(np_max((g - R(1)) * (hroe - keroe), R(kFloor)));
@@ -192,25 +238,28 @@ __device__ __forceinline__ void hllc(const R* ul, const R* ur, R gl, R gr, R* ou
   const R sL = np_min(unl - al, uroe - aroe);
   const R sR = np_max(unr + ar, uroe + aroe);
   const R den = guarded(rl * (sL - unl) - rr * (sR - unr), R(kGuard));
-  const R ss = (((pr - pl) + (rl * unl) * (sL - unl)) - (rr * unr) * (sR - unr)) / den;
+  const R ss = dv(((pr - pl) + (rl * unl) * (sL - unl)) - (rr * unr) * (sR - unr), den);
 
   // star state of the side whose star region can be selected
   const bool right = (ss <= R(0));
-  const R* u = right ? ur : ul;
-  const R* fs = right ? fr : fl;
   const R rho = right ? rr : rl;
   const R un = right ? unr : unl;
   const R p = right ? pr : pl;
   const R s = right ? sR : sL;
+  const R uE = right ? ur[E] : ul[E];
   const R dss = guarded(s - ss, R(kGuard));
-  const R rho_s = np_max(rho * ((s - un) / dss), R(kFloor));
+  const R rho_s = np_max(rho * dv(s - un, dss), R(kFloor));
   const R dun = guarded(s - un, R(kGuard));
   R star[NV];
   star[0] = rho_s;
   star[1] = rho_s * ss;
 #pragma unroll
   for (int t = 0; t < NT; ++t) star[2 + t] = rho_s * (right ? utr[t] : utl[t]);
-  star[E] = rho_s * (u[E] / rho + (ss - un) * (ss + p / (rho * dun)));
+  if constexpr (X) {
+    star[E] = rho_s * (uE / rho + (ss - un) * (ss + p / (rho * dun)));
+  } else {
+    star[E] = rho_s * (uE * (right ? irr : irl) + (ss - un) * (ss + dv(p, rho * dun)));
+  }
   const bool close = fabs(s - ss) < R(kFloor);
 
   const bool mr = (R(0) >= sR);
@@ -219,7 +268,9 @@ __device__ __forceinline__ void hllc(const R* ul, const R* ur, R gl, R gr, R* ou
   const bool ml = (R(0) <= sL);
 #pragma unroll
   for (int c = 0; c < NV; ++c) {
-    const R fstar = close ? fs[c] : fs[c] + s * (star[c] - u[c]);
+    const R uc = right ? ur[c] : ul[c];
+    const R fc = right ? fr[c] : fl[c];
+    const R fstar = close ? fc : fc + s * (star[c] - uc);
     R v = R(NAN);
     if (ml) v = fl[c];
     if (msl || msr) v = fstar;

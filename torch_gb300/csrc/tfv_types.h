@@ -21,6 +21,7 @@ struct InstDesc {
   int32_t controller, variant, wavespeed;  // 1D options
   int32_t tile0, ntiles; // range of this instance in the tile table
   int32_t has_flux_out;
+  int32_t tma;           // tensor maps of this instance's buffers are valid
   int64_t ncell;
   int64_t max_steps;
   double h[3];
@@ -51,7 +52,8 @@ struct InstState {
   int32_t last_fallback;
   int32_t retry;         // reactive dt halvings taken in this step
   double dt_allowed;     // reactive: CFL dt of the half-reacted state
-  double pad_;
+  double coef_half[3];   // (0.5*dt)/h_d, predictor coefficients
+  double coef_full[3];   // dt/h_d, update coefficients
 };
 
 // One tile of work: an in-plane block of one instance over a chunk of
@@ -72,6 +74,9 @@ struct StepArgs {
   int32_t ninst;
   int32_t src_off;  // ring offset (from cur) of the state a kernel reads
   int32_t dst_off;  // ring offset of the state it writes
+  int32_t t_begin;  // tile range of this launch
+  int32_t t_end;
+  const void* tmaps;  // [ninst][4] CUtensorMap (128 B each): ring buffers 0..2, gamma
   double* t_bsum;  // [ntiles][3][5] boundary face sums per direction
   double* t_wmax;  // [ntiles][3] max(|u_d| + a) of the new state
   double* t_sum;   // [ntiles][5] integrals / source partial sums

@@ -105,7 +105,9 @@ class _Engine:
         handle = C.c_void_p()
         t = None
         if tile is not None:
-            t = _lib.Tile(*tile)
+            # (tx, ty, chunk[, persistent_ctas[, tma]]); tensor-copy staging on by default
+            vals = list(tile) + [0, 1][len(tile) - 3:] if len(tile) < 5 else list(tile)
+            t = _lib.Tile(*vals[:5])
         _lib.check(lib.tfv_batch_create(dim, _lib.TFV_FP64 if precision == "fp64" else _lib.TFV_FP32,
                                         self.n, arr, C.byref(t) if t is not None else None,
                                         C.byref(handle)))
