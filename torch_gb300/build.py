@@ -24,9 +24,11 @@ LIB = BUILD / "libtfv.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + str(INCLUDE),
           "-I" + str(CSRC)]
+F32 = ["-fmad=true", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
 UNITS = {
     "tfv_f64.cu": ["-fmad=false"],
-    "tfv_f32.cu": ["-fmad=true", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
+    "tfv_f32_3d.cu": F32,
+    "tfv_f32_2d.cu": F32,
     "tfv_host.cu": [],
 }
 

@@ -1,0 +1,8 @@
+// Single-precision 2D step kernels (see tfv_f32_3d.cu).
+#define REAL float
+#define TFV_HYDRO_MIN_BLOCKS 3
+#define TFV_FIXED_SHAPES 1
+#define TFV_WITH_2D 1
+#define TFV_WITH_3D 0
+#define TFV_LAUNCH2_NAME launch_step2_f32
+#include "tfv_inst.inc"

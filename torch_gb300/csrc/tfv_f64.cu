@@ -1,11 +1,14 @@
 // Double-precision step kernels: the reference-faithful path.  Built with
 // -fmad=false so every product and sum rounds separately, as in NumPy.
 #define REAL double
+#define TFV_DEFINE_SHARED_KERNELS
 // double precision needs ~250 registers; one CTA bound, 128-thread tiles
 #define TFV_HYDRO_MIN_BLOCKS 1
-#define TFV_DEFINE_SHARED_KERNELS
-#define TFV_LAUNCH_NAME launch_step_f64
-#define TFV_SMEM_NAME hydro_smem_f64
+#define TFV_FIXED_SHAPES 0
+#define TFV_WITH_2D 1
+#define TFV_WITH_3D 1
+#define TFV_LAUNCH2_NAME launch_step2_f64
+#define TFV_LAUNCH3_NAME launch_step3_f64
 #define TFV_HLLC_NAME launch_hllc_f64
 #include "tfv_inst.inc"
 

@@ -276,8 +276,10 @@ cudaError_t launch_range(tfv_batch* b, int op, int lim, int t0, int t1, int src_
   A.t_end = t1;
   const int grid = grid_for(b, t1 - t0);
   if (b->precision == TFV_FP64)
-    return launch_step_f64(op, b->dim, b->varg, lim, A, grid, b->block, b->stream);
-  return launch_step_f32(op, b->dim, b->varg, lim, A, grid, b->block, b->stream);
+    return b->dim == 3 ? launch_step3_f64(op, b->varg, lim, A, grid, b->block, b->stream)
+                       : launch_step2_f64(op, b->varg, lim, A, grid, b->block, b->stream);
+  return b->dim == 3 ? launch_step3_f32(op, b->varg, lim, A, grid, b->block, b->stream)
+                     : launch_step2_f32(op, b->varg, lim, A, grid, b->block, b->stream);
 }
 
 // The step kernel is instantiated per limiter: one launch per limiter group.

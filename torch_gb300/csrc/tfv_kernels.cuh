@@ -849,13 +849,15 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   return true;
 }
 
-template <typename R, int DIM, bool VARG, int LIM>
+// TX, TY > 0: tile shape fixed at compile time (shared-memory offsets become
+// immediates); 0: taken from the launch arguments.
+template <typename R, int DIM, bool VARG, int LIM, int TX, int TY>
 __global__ void __launch_bounds__(256, TFV_HYDRO_MIN_BLOCKS) hydro_kernel(StepArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
   HydroSmem<R, DIM, VARG> S;
-  S.init(A.tx, A.ty);
+  S.init(TX > 0 ? TX : A.tx, TY > 0 ? TY : A.ty);
   if (threadIdx.x == 0) {
     uint64_t* bars = smem_at<uint64_t>(smem, S.bar_off);
     for (int k = 0; k < 3; ++k) mbar_init(bars + k, 1);

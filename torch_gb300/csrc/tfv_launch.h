@@ -12,12 +12,14 @@ namespace tfv {
 enum : int { kOpHydro = 0, kOpFallback = 1, kOpWaves = 2 };
 
 // lim selects the limiter instantiation of the step kernel (ignored otherwise).
-cudaError_t launch_step_f64(int op, int dim, bool varg, int lim, const StepArgs& A, int grid,
-                            int block, cudaStream_t s);
-cudaError_t launch_step_f32(int op, int dim, bool varg, int lim, const StepArgs& A, int grid,
-                            int block, cudaStream_t s);
-size_t hydro_smem_f64(int dim, bool varg, int tx, int ty);
-size_t hydro_smem_f32(int dim, bool varg, int tx, int ty);
+cudaError_t launch_step2_f64(int op, bool varg, int lim, const StepArgs& A, int grid, int block,
+                             cudaStream_t s);
+cudaError_t launch_step3_f64(int op, bool varg, int lim, const StepArgs& A, int grid, int block,
+                             cudaStream_t s);
+cudaError_t launch_step2_f32(int op, bool varg, int lim, const StepArgs& A, int grid, int block,
+                             cudaStream_t s);
+cudaError_t launch_step3_f32(int op, bool varg, int lim, const StepArgs& A, int grid, int block,
+                             cudaStream_t s);
 cudaError_t launch_hllc_f64(int nv, int64_t n, const void* ul, const void* ur, const void* gl,
                             const void* gr, void* out, cudaStream_t s);
 cudaError_t launch_hllc_f32(int nv, int64_t n, const void* ul, const void* ur, const void* gl,
