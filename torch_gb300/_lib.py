@@ -23,8 +23,9 @@ VARIANTS = {"Variante 1 - Original": 0, "Variante_2": 1}
 WAVESPEEDS = {"Pressure Based": 0, "Enthalpy Based": 1}
 
 STATUS = {0: "READY", 1: "DONE", 2: "ERR_MAXSTEPS", 3: "ERR_STALL", 4: "ERR_NONPHYSICAL",
-          5: "ERR_REACTIVE", 6: "ERR_SPECIES", 7: "ERR_CHEMISTRY", 8: "RETRY"}
-READY, DONE = 0, 1
+          5: "ERR_REACTIVE", 6: "ERR_SPECIES", 7: "ERR_CHEMISTRY", 8: "RETRY",
+          9: "ERR_DEVICE_WAIT"}
+READY, DONE, ERR_CHEMISTRY, RETRY, ERR_DEVICE_WAIT = 0, 1, 7, 8, 9
 STATUS_MESSAGES = {
     2: "Maximum steps reached before requested final time",
     3: "Integration stalled before requested final time",
@@ -32,6 +33,7 @@ STATUS_MESSAGES = {
     5: "Could not find stable reactive step",
     6: "3D scalar transport left the physical interval",
     7: "Reaction requires a physical state and reactant fractions in [0,1]",
+    9: "A device-side wait on a tensor copy timed out",
 }
 
 

@@ -65,6 +65,7 @@ struct tfv_batch {
          off_flags = 0, off_int = 0, off_gam = 0, off_tmaps = 0, total = 0;
   std::vector<CUtensorMap> tmaps;  // [n][4]: ring buffers 0..2, gamma
   size_t gam_bytes = 0;
+  size_t off_mflux = 0, mflux_bytes = 0;
   unsigned char* ws = nullptr;
   cudaStream_t stream = nullptr;
   StepArgs args{};
@@ -208,6 +209,17 @@ void layout(tfv_batch* b) {
     for (int i = 0; i < b->n; ++i) b->gam_bytes += align_up(real_size(b->precision) * b->desc[i].ncell, 256);
   }
   o += b->gam_bytes;
+  o = align_up(o, 256);
+  b->off_mflux = o;
+  b->mflux_bytes = 0;
+  if (b->reactive) {  // face mass fluxes of the hydro step, read by the species transport
+    for (int i = 0; i < b->n; ++i) {
+      const InstDesc& d = b->desc[i];
+      for (int k = 0; k < b->dim; ++k)
+        b->mflux_bytes += align_up(real_size(b->precision) * (d.ncell / d.n[k]) * (d.n[k] + 1), 256);
+    }
+  }
+  o += b->mflux_bytes;
   b->total = align_up(o, 256);
 }
 
@@ -301,8 +313,24 @@ cudaError_t finalize(tfv_batch* b, int mode, int dst_off) {
                          reinterpret_cast<double*>(b->ws + b->off_int), b->stream);
 }
 
-// Enqueue one complete non-reactive step for every READY instance.
+// Enqueue one complete step for every READY instance.  Reactive steps
+// (python/cfdSolver/torchSession.py:401-517): half reaction from the start
+// state (ring cur -> cur+1) and the CFL check, which may halve dt and leave
+// the instance in RETRY (the next enqueued step retries from the start
+// state); hydro on the heated state (cur+1 -> cur+2) with its mass fluxes;
+// species transport; second half reaction (cur+2 -> cur+1) with the source
+// sums; commit (cur <- cur+1).
 cudaError_t enqueue_step(tfv_batch* b) {
+  if (b->reactive) {
+    cudaError_t e = launch(b, kOpReact1, 0, 1);
+    if (e == cudaSuccess) e = finalize(b, 4, 1);
+    if (e == cudaSuccess) e = launch(b, kOpHydro, 1, 2);
+    if (e == cudaSuccess) e = launch(b, kOpFallback, 1, 2);
+    if (e == cudaSuccess) e = launch(b, kOpSpecies, 1, 2);
+    if (e == cudaSuccess) e = launch(b, kOpReact2, 2, 1);
+    if (e == cudaSuccess) e = finalize(b, 0, 1);
+    return e;
+  }
   cudaError_t e = launch(b, kOpHydro, 0, 1);
   if (e != cudaSuccess) return e;
   e = launch(b, kOpFallback, 0, 1);
@@ -340,7 +368,19 @@ static int create_internal(int32_t dim, int32_t precision, int32_t n, const tfv_
   for (int i = 0; i < n; ++i) {
     const int r = validate(cfgs[i], dim);
     if (r != TFV_OK) return r;
-    if (cfgs[i].reactive) return fail(TFV_EINVAL, "reactive batches are not supported yet");
+    if (cfgs[i].reactive != cfgs[0].reactive || cfgs[i].closure != cfgs[0].closure)
+      return fail(TFV_EINVAL, "a batch holds only reactive or only inert instances of one closure");
+    if (cfgs[i].reactive) {
+      const tfv_config& c = cfgs[i];
+      if (!(std::isfinite(c.q_heat) && std::isfinite(c.activation) &&
+            std::isfinite(c.pre_exponential)) ||
+          c.q_heat < 0 || c.activation < 0 || c.pre_exponential < 0)
+        return fail(TFV_EINVAL, "Reaction time and constants must be finite and nonnegative");
+      if (c.kinetic_model != TFV_ARRHENIUS && c.kinetic_model != TFV_ZND)
+        return fail(TFV_EINVAL, "Unknown limiter or chemistry model");
+      if (c.closure != TFV_CLOSURE_SI && c.closure != TFV_CLOSURE_NONDIM)
+        return fail(TFV_EINVAL, "Unknown chemistry closure");
+    }
   }
   tfv_batch* b = new tfv_batch();
   b->dim = dim;
@@ -374,8 +414,11 @@ static int create_internal(int32_t dim, int32_t precision, int32_t n, const tfv_
                 "tile shape must have tx >= 4, ty >= 1, chunk >= 1, tx*ty a multiple of 32 "
                 "and at most 256");
   }
-  b->varg = varg;
-  b->nring = 2;
+  b->reactive = cfgs[0].reactive != 0;
+  // reactive SI closure: gamma(lambda) per cell, computed into the workspace
+  b->own_gamma = b->reactive && cfgs[0].closure == TFV_CLOSURE_SI;
+  b->varg = varg || b->own_gamma;
+  b->nring = b->reactive ? 3 : 2;
   b->desc.resize(n);
   for (int i = 0; i < n; ++i) fill_desc(b, i);
   build_tiles(b);
@@ -413,6 +456,30 @@ int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* con
       d.beta[k] = betas ? betas[i * b->nring + k] : nullptr;
     }
     d.has_flux_out = 0;
+    d.flux_nv = b->dim + 2;
+    if (b->reactive && (!d.lam[0] || !d.lam[1] || !d.lam[2]))
+      return fail(TFV_EINVAL, "reactive instances need lambda ring buffers");
+    if (b->reactive && b->cfg[i].kinetic_model == TFV_ZND && (!d.beta[0] || !d.beta[1] || !d.beta[2]))
+      return fail(TFV_EINVAL, "ZND instances need beta ring buffers");
+  }
+  {
+    size_t og = b->off_gam, om = b->off_mflux;
+    for (int i = 0; i < b->n; ++i) {
+      InstDesc& d = b->desc[i];
+      if (b->own_gamma) {
+        d.gam = b->ws + og;
+        og += align_up(real_size(b->precision) * d.ncell, 256);
+      }
+      if (b->reactive) {
+        for (int k = 0; k < 3; ++k) d.flux_out[k] = nullptr;
+        for (int k = 0; k < b->dim; ++k) {
+          d.flux_out[k] = b->ws + om;
+          om += align_up(real_size(b->precision) * (d.ncell / d.n[k]) * (d.n[k] + 1), 256);
+        }
+        d.has_flux_out = 1;
+        d.flux_nv = 1;
+      }
+    }
   }
   b->tmaps.assign((size_t)b->n * 4, CUtensorMap{});
   for (int i = 0; i < b->n; ++i) {
@@ -452,6 +519,7 @@ int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* con
                            sizeof(CUtensorMap) * b->tmaps.size(), cudaMemcpyHostToDevice,
                            b->stream));
   // initial integrals and first dt
+  if (b->own_gamma) TFV_CUDA(launch(b, kOpGamma, 0, 0));
   TFV_CUDA(launch(b, kOpWaves, 0, 0));
   TFV_CUDA(finalize(b, 3, 0));
   TFV_CUDA(cudaStreamSynchronize(b->stream));
@@ -527,6 +595,7 @@ int tfv_batch_report(tfv_batch* b, tfv_report* out) {
 int tfv_batch_integrals(tfv_batch* b, double* out) {
   int r = check_bound(b);
   if (r) return r;
+  if (b->own_gamma) TFV_CUDA(launch(b, kOpGamma, 0, 0));
   TFV_CUDA(launch(b, kOpWaves, 0, 0));
   TFV_CUDA(finalize(b, 2, 0));
   TFV_CUDA(cudaMemcpyAsync(out, b->ws + b->off_int, sizeof(double) * 5 * b->n,
@@ -538,6 +607,7 @@ int tfv_batch_integrals(tfv_batch* b, double* out) {
 int tfv_batch_replan(tfv_batch* b) {
   int r = check_bound(b);
   if (r) return r;
+  if (b->own_gamma) TFV_CUDA(launch(b, kOpGamma, 0, 0));
   TFV_CUDA(launch(b, kOpWaves, 0, 0));
   TFV_CUDA(finalize(b, 1, 0));
   return TFV_OK;
@@ -547,6 +617,8 @@ int tfv_batch_set_flux_outputs(tfv_batch* b, int32_t inst, void* fx, void* fy, v
   int r = check_bound(b);
   if (r) return r;
   if (inst < 0 || inst >= b->n) return fail(TFV_EINVAL, "instance out of range");
+  if (b->reactive)
+    return fail(TFV_EINVAL, "reactive batches use the flux buffers for species transport");
   InstDesc& d = b->desc[inst];
   d.flux_out[0] = fx;
   d.flux_out[1] = fy;

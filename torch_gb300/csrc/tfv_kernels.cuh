@@ -607,6 +607,7 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   bool bad = false, gate = false;
   R* fout[3] = {(R*)d.flux_out[0], (R*)d.flux_out[1], (R*)d.flux_out[2]};
   const bool want_flux = d.has_flux_out != 0;
+  const int nvo = d.flux_nv;
 
   // domain corners of the active box that this tile must gate (3D)
   int ncorner = 0;
@@ -739,7 +740,7 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
             const int64_t nf = (int64_t)g.na + 1;
 #pragma unroll
             for (int c = 0; c < NV; ++c)
-              fout[0][((int64_t)(c * g.np + it) * g.nb + (y0 + b)) * nf + x0 + af] = F[c];
+              if (c < nvo) fout[0][((int64_t)(c * g.np + it) * g.nb + (y0 + b)) * nf + x0 + af] = F[c];
           }
         } else {
           const int a = i, bf = j;
@@ -756,7 +757,7 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
           if (want_flux && fout[1]) {
 #pragma unroll
             for (int c = 0; c < NV; ++c)
-              fout[1][((int64_t)(c * g.np + it) * (g.nb + 1) + (y0 + bf)) * g.na + x0 + a] = F[c];
+              if (c < nvo) fout[1][((int64_t)(c * g.np + it) * (g.nb + 1) + (y0 + bf)) * g.na + x0 + a] = F[c];
           }
         }
       }
@@ -777,7 +778,7 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
         if (want_flux && fout[MD]) {
 #pragma unroll
           for (int c = 0; c < NV; ++c)
-            fout[MD][((int64_t)(c * (g.np + 1) + it) * g.nb + (y0 + ob)) * g.na + x0 + oa] = Fm[c];
+            if (c < nvo) fout[MD][((int64_t)(c * (g.np + 1) + it) * g.nb + (y0 + ob)) * g.na + x0 + oa] = Fm[c];
         }
         if (it > p0) {
           R un[NV];
@@ -1003,6 +1004,7 @@ __global__ void __launch_bounds__(256) fallback_kernel(StepArgs A) {
             (void)fp_n;
 #pragma unroll
             for (int c = 0; c < NV; ++c) {
+              if (c >= d.flux_nv) continue;
               const int64_t base = (int64_t)c * (dd == DIM - 1 ? g.np + 1 : g.np);
               fout[dd][((base + p) * fb_n + b) * fa_n + a] = Fm[c];
               if (idx == n - 1)
@@ -1103,23 +1105,20 @@ __global__ void __launch_bounds__(256) waves_kernel(StepArgs A) {
 // Per-instance finalize: commit the step (ring swap, boundary integral,
 // time, steps), then plan the next dt (python/cfdSolver/torchSession.py:
 // 379-396, 498-522).  mode 0: commit + plan; 1: plan only; 2: integrals only;
-// 3: record the initial integrals, then plan (bind).  One CTA per instance.
+// 3: record the initial integrals, then plan (bind); 4: reactive dt check
+// after the first half reaction (accept, or halve dt and retry, at most 60
+// attempts; torchSession.py:401-411).  One CTA per instance.
 // --------------------------------------------------------------------------
-__device__ __forceinline__ void plan_next(const InstDesc& d, InstState& st, const double* w,
-                                          int fp32) {
-  if (st.time == d.t_end) {
-    st.status = kDone;
-    return;
-  }
-  if (st.steps >= d.max_steps) {
-    st.status = kErrMaxSteps;
-    return;
-  }
-  double dt;
+// CFL dt from the wave-speed maxima w (python/cfdSolver/torchSession.py:333-360):
+// 3D cfl / sum_d max(|u_d|+a)/h_d; 2D on floored primitives including the
+// inlet ghost rows, 1e-3 when the speeds vanish; 1D min of the wave-speed and
+// hydro estimates (w[0] = max |S|, w[1] = max(|u| + a)).
+__device__ __forceinline__ double cfl_dt(const InstDesc& d, const double* w) {
   if (d.dim == 3) {
     const double total = (w[0] / d.h[0] + w[1] / d.h[1]) + w[2] / d.h[2];
-    dt = d.cfl / total;
-  } else if (d.dim == 2) {
+    return d.cfl / total;
+  }
+  if (d.dim == 2) {
     double w0 = w[0], w1 = w[1];
     if (d.bc[1] == kBcInflow) {  // the inlet ghost rows take part in the 2D dt
       const double rho = fmax(d.inlet[0], 1e-12);
@@ -1130,26 +1129,313 @@ __device__ __forceinline__ void plan_next(const InstDesc& d, InstState& st, cons
       w1 = fmax(w1, fabs(vy) + a);
     }
     const double total = w0 / d.h[0] + w1 / d.h[1];
-    dt = total <= 1e-12 ? 1e-3 : d.cfl / total;
-  } else {
-    // 1D: w[0] = max |S| over faces, w[1] = max(|u| + a) over padded cells
-    const double dw = w[0] > 0 ? (d.cfl * d.h[0]) / w[0] : 1e-6;
-    const double dh = d.cfl * d.h[0] / w[1];
-    dt = dh < dw ? dh : dw;
+    return total <= 1e-12 ? 1e-3 : d.cfl / total;
   }
-  if (fp32) dt = (double)(float)dt;
-  const double rem = d.t_end - st.time;
-  if (rem < dt) dt = rem;
+  const double dw = w[0] > 0 ? (d.cfl * d.h[0]) / w[0] : 1e-6;
+  const double dh = d.cfl * d.h[0] / w[1];
+  return dh < dw ? dh : dw;
+}
+
+__device__ __forceinline__ void set_dt(const InstDesc& d, InstState& st, double dt) {
   st.dt = dt;
   for (int k = 0; k < 3; ++k) {
     st.coef_half[k] = (0.5 * dt) / d.h[k];
     st.coef_full[k] = dt / d.h[k];
   }
+}
+
+__device__ __forceinline__ void plan_next(const InstDesc& d, InstState& st, const double* w,
+                                          int fp32) {
+  if (st.time == d.t_end) {
+    st.status = kDone;
+    return;
+  }
+  if (st.steps >= d.max_steps) {
+    st.status = kErrMaxSteps;
+    return;
+  }
+  double dt = cfl_dt(d, w);
+  if (fp32) dt = (double)(float)dt;
+  const double rem = d.t_end - st.time;
+  if (rem < dt) dt = rem;
+  set_dt(d, st, dt);
   if (!isfinite(dt) || dt <= 0.0 || st.time + dt == st.time) {
     st.status = kErrStall;
     return;
   }
   st.status = kReady;
+}
+
+// --------------------------------------------------------------------------
+// Chemistry: exponential-midpoint Arrhenius / two-stage ZND source on the
+// 1D projection of a cell (python/cfdSolver/torchSolver.py:708-789 via
+// reaction_step_2d / reaction_step_3d, torchSolver2D.py:474-509,
+// torchSolver3D.py:225-243).  Closure SI: gamma(lambda), T = p M / (rho R_u),
+// rate = A exp(-Ea / (8.314 T)); closure nondimensional: constant gamma,
+// T = p / rho, rate = A exp(-Ea_over_R / T).
+// --------------------------------------------------------------------------
+__device__ __forceinline__ double texp(double x) { return exp(x); }
+__device__ __forceinline__ float texp(float x) { return expf(x); }
+
+template <typename R>
+__device__ __forceinline__ R gamma_of_lambda(R lam) {
+  return (R(4.5) - lam) / (R(3.5) - lam);
+}
+
+template <typename R>
+__device__ __forceinline__ R reaction_rate(const InstDesc& d, R lam, R s0, R s1, R s2) {
+  const bool si = d.closure == 0;
+  const R g = si ? gamma_of_lambda(lam) : R(d.gamma);
+  // uconsv_to_uprim (torchSolver.py:117-127)
+  const R rho = np_max(s0, R(kFloor));
+  const R u = s1 / rho;
+  const R p = np_max((s2 - (R(0.5) * rho) * (u * u)) * (g - R(1)), R(kFloor));
+  R t;
+  if (si) {
+    // temp_calc (torchSolver.py:90-114)
+    const R rho2 = np_max(rho, R(kFloor));
+    const R molar = (lam * R(2.0 / 3.0)) * R(2.016) + (lam * R(1.0 / 3.0)) * R(32.0) +
+                    (R(1) - lam) * R(18.016);
+    t = np_max((p * molar) / (rho2 * R(8314.46)), R(kFloor));
+    return R(d.a) * texp(-R(d.ea) / (R(8.314) * t));
+  }
+  t = np_max(p / rho, R(kFloor));
+  return R(d.a) * texp(-R(d.ea) / t);
+}
+
+// One cell: returns false when the reference would reject the input
+// (reactant fraction outside [0,1] or not finite, nonphysical 1D state,
+// induction fraction outside [0,1]).
+template <typename R, int DIM>
+__device__ __forceinline__ bool react_cell(const InstDesc& d, R* u, R& lam, R& beta, bool znd,
+                                           double dt_r) {
+  constexpr int NV = DIM + 2;
+  const R s0 = u[0], s1 = u[1];
+  R st = u[2] * u[2];
+  if (DIM == 3) st = st + u[3] * u[3];
+  const R s2 = u[NV - 1] - (R(0.5) * st) / u[0];
+  bool ok = finite_(lam) && lam >= R(0) && lam <= R(1);
+  const R e1 = s2 - (R(0.5) * (s1 * s1)) / s0;
+  ok = ok && finite_(s0) && finite_(s1) && finite_(s2) && s0 > R(kFloor) && e1 > R(kFloor);
+  const R beta_n = znd ? beta : R(1);
+  if (znd) ok = ok && finite_(beta) && beta >= R(0) && beta <= R(1);
+  const R q = R(d.q);
+  const R lam_n = lam;
+  auto advance = [&](R rate, R duration, R& lam_out, R& beta_out) {
+    if (znd) {
+      const R floor_rate = Exact<R>::value ? R(1e-300) : R(1e-30);
+      const R active = np_max(R(0), duration - beta_n / np_max(rate, floor_rate));
+      lam_out = lam_n * texp((R(-5.0) * rate) * active);
+      beta_out = np_min(np_max(beta_n - rate * duration, R(0)), R(1));
+    } else {
+      lam_out = lam_n * texp((-rate) * duration);
+      beta_out = R(0);
+    }
+  };
+  R lam_mid, beta_mid;
+  advance(reaction_rate<R>(d, lam_n, s0, s1, s2), R(0.5 * dt_r), lam_mid, beta_mid);
+  const R s2_mid = s2 + (q * s0) * (lam_n - lam_mid);
+  R lam_new, beta_new;
+  advance(reaction_rate<R>(d, lam_mid, s0, s1, s2_mid), R(dt_r), lam_new, beta_new);
+  const R s2_new = s2 + (q * s0) * (lam_n - lam_new);
+  u[NV - 1] = u[NV - 1] + (s2_new - s2);
+  lam = lam_new;
+  if (znd) beta = beta_new;
+  return ok;
+}
+
+// Reaction half step over every tile.  stage 1: start (ring cur) -> heated
+// (cur+1) and gamma(lambda) for the hydro step; wave maxima for the reactive
+// dt check.  stage 2: hydro (cur+2) -> new (cur+1, where the heated state
+// was), source partial sums (old - start + new - hydro) and the wave maxima of
+// the new state for the next dt (python/cfdSolver/torchSession.py:401-411,
+// 510-517).
+template <typename R, int DIM, bool VARG>
+__global__ void __launch_bounds__(256) react_kernel(StepArgs A, int stage) {
+  constexpr int NV = DIM + 2;
+  __shared__ double red[40];
+  for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
+    const Tile T = A.tiles[t];
+    const InstDesc& d = A.desc[T.inst];
+    InstState& st = A.st[T.inst];
+    const int status = st.status;
+    if (!(status == kReady || (stage == 1 && status == kRetry))) continue;  // uniform
+    Geo<DIM> g;
+    g.init(d);
+    const int cur = st.cur;
+    const int i0 = cur % d.nring, i1 = (cur + 1) % d.nring, i2 = (cur + 2) % d.nring;
+    const R* Usrc = (const R*)d.U[stage == 1 ? i0 : i2];
+    R* Udst = (R*)d.U[i1];
+    const R* Ustart = (const R*)d.U[i0];
+    const R* Lsrc = (const R*)d.lam[stage == 1 ? i0 : i2];
+    R* Ldst = (R*)d.lam[i1];
+    const bool znd = d.model == 1;
+    const R* Bsrc = znd ? (const R*)d.beta[stage == 1 ? i0 : i2] : nullptr;
+    R* Bdst = znd ? (R*)d.beta[i1] : nullptr;
+    R* gam = VARG ? (R*)d.gam : nullptr;
+    const double half = 0.5 * st.dt;
+    const int ax = min(A.tx, g.na - T.x0);
+    const int by = DIM == 3 ? min(A.ty, g.nb - T.y0) : 1;
+    const bool owner = (int)threadIdx.x < ax * by;
+    const int a = T.x0 + (owner ? (int)threadIdx.x % ax : 0);
+    const int b = DIM == 3 ? T.y0 + (owner ? (int)threadIdx.x / ax : 0) : 0;
+    R wmax[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) wmax[k] = R(0);
+    double src[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) src[c] = 0.0;
+    int fl = 0;
+    if (owner) {
+      for (int p = T.p0; p < T.p1; ++p) {
+        const int64_t off = (int64_t)p * g.ps + (int64_t)b * g.na + a;
+        R u[NV], hyd[NV];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+          u[c] = Usrc[c * g.cs + off];
+          hyd[c] = u[c];
+        }
+        R lam = Lsrc[off];
+        R beta = znd ? Bsrc[off] : R(1);
+        if (!react_cell<R, DIM>(d, u, lam, beta, znd, half)) fl |= kFlagChemistry;
+        if (stage == 2) {
+#pragma unroll
+          for (int c = 0; c < NV; ++c) {
+            const double old = (double)Udst[c * g.cs + off];  // heated state of this step
+            const double start = (double)Ustart[c * g.cs + off];
+            src[c] += ((old - start) + (double)u[c]) - (double)hyd[c];
+          }
+          if (!physical_cell<R, NV>(u)) fl |= kFlagNonphysical;
+        }
+#pragma unroll
+        for (int c = 0; c < NV; ++c) Udst[c * g.cs + off] = u[c];
+        Ldst[off] = lam;
+        if (znd) Bdst[off] = beta;
+        const R gc = (d.closure == 0) ? gamma_of_lambda(lam) : R(d.gamma);
+        if (VARG && stage == 1) gam[off] = gc;
+        R w[DIM];
+        wave_speeds<R, DIM>(u, gc, w);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) wmax[k] = fmax(wmax[k], w[k]);
+      }
+    }
+    fl = block_or(fl, reinterpret_cast<int*>(red));
+    double wm[DIM], sm[NV];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) wm[k] = block_max(owner ? (double)wmax[k] : 0.0, red);
+#pragma unroll
+    for (int c = 0; c < NV; ++c) sm[c] = stage == 2 ? block_sum(src[c], red) : 0.0;
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < DIM; ++k) A.t_wmax[(size_t)t * 3 + k] = wm[k];
+      if (stage == 2) {
+        for (int c = 0; c < NV; ++c) A.t_sum[(size_t)t * 5 + c] = sm[c];
+        A.t_flags[t] |= fl;
+      } else {
+        A.t_flags[t] = fl;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Species transport with the hydro mass fluxes: first-order upwind in every
+// direction (python/cfdSolver/torchSolver3D.py:246-256,
+// torchSolver2D.py:659-667).  q = lambda (and beta) of the heated state
+// (ring cur+1) -> ring cur+2.  Scalar ghost cells: no sign change; the 2D
+// inlet rows hold fresh mixture (1).
+template <typename R, int DIM>
+__device__ __forceinline__ R fetch_scalar(const InstDesc& d, const Geo<DIM>& g, const R* q, int a,
+                                          int b, int p) {
+  bool ga, gb = false, gp;
+  const int sa = map_axis(a, g.na, g.bca, ga);
+  const int sb = DIM == 3 ? map_axis(b, g.nb, g.bcb, gb) : 0;
+  const int sp = map_axis(p, g.np, g.bcp, gp);
+  if (DIM == 2 && g.bcp == kBcInflow && p < 0) return R(1);
+  return q[(int64_t)sp * g.ps + (int64_t)sb * g.na + sa];
+}
+
+template <typename R, int DIM>
+__global__ void __launch_bounds__(256) species_kernel(StepArgs A) {
+  __shared__ int red[40];
+  for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
+    const Tile T = A.tiles[t];
+    const InstDesc& d = A.desc[T.inst];
+    InstState& st = A.st[T.inst];
+    if (st.status != kReady) continue;  // uniform
+    Geo<DIM> g;
+    g.init(d);
+    const int cur = st.cur;
+    const int i1 = (cur + 1) % d.nring, i2 = (cur + 2) % d.nring;
+    const R* Uold = (const R*)d.U[i1];
+    const R* Unew = (const R*)d.U[i2];
+    const int nq = d.model == 1 ? 2 : 1;
+    const R* mf[3] = {(const R*)d.flux_out[0], (const R*)d.flux_out[1], (const R*)d.flux_out[2]};
+    R cu[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) cu[k] = R(st.coef_full[k]);
+    const int ax = min(A.tx, g.na - T.x0);
+    const int by = DIM == 3 ? min(A.ty, g.nb - T.y0) : 1;
+    const bool owner = (int)threadIdx.x < ax * by;
+    const int a = T.x0 + (owner ? (int)threadIdx.x % ax : 0);
+    const int b = DIM == 3 ? T.y0 + (owner ? (int)threadIdx.x / ax : 0) : 0;
+    int fl = 0;
+    if (owner) {
+      for (int s = 0; s < nq; ++s) {
+        const R* q = (const R*)(s == 0 ? d.lam[i1] : d.beta[i1]);
+        R* qn = (R*)(s == 0 ? d.lam[i2] : d.beta[i2]);
+        for (int p = T.p0; p < T.p1; ++p) {
+          const int64_t off = (int64_t)p * g.ps + (int64_t)b * g.na + a;
+          const R qc = q[off];
+          R rhoq = Uold[off] * qc;
+#pragma unroll
+          for (int dd = 0; dd < DIM; ++dd) {
+            const int ia = dd == 0 ? 1 : 0;
+            const int ib = (DIM == 3 && dd == 1) ? 1 : 0;
+            const int ip = dd == DIM - 1 ? 1 : 0;
+            // face arrays of this direction have one more entry along dd
+            const int fa_n = dd == 0 ? g.na + 1 : g.na;
+            const int fb_n = (DIM == 3 && dd == 1) ? g.nb + 1 : g.nb;
+            const int64_t lo = ((int64_t)p * fb_n + b) * fa_n + a;
+            const int64_t hi = ((int64_t)(p + ip) * fb_n + b + ib) * fa_n + a + ia;
+            const R Flo = mf[dd][lo], Fhi = mf[dd][hi];
+            const R qlo_l = fetch_scalar<R, DIM>(d, g, q, a - ia, b - ib, p - ip);
+            const R qhi_r = fetch_scalar<R, DIM>(d, g, q, a + ia, b + ib, p + ip);
+            const R Glo = Flo * (Flo >= R(0) ? qlo_l : qc);
+            const R Ghi = Fhi * (Fhi >= R(0) ? qc : qhi_r);
+            rhoq = rhoq - cu[dd] * (Ghi - Glo);
+          }
+          R frac;
+          if (DIM == 3) {
+            // the reference's interval check; FP32 roundoff needs a wider margin
+            const R tol = Exact<R>::value ? R(1e-10) : R(1e-5);
+            frac = rhoq / Unew[off];
+            if (frac < -tol || frac > R(1) + tol) fl |= kFlagSpecies;
+          } else {
+            frac = rhoq / np_max(Unew[off], R(kFloor));
+          }
+          qn[off] = np_min(np_max(frac, R(0)), R(1));
+        }
+      }
+    }
+    fl = block_or(fl, red);
+    if (threadIdx.x == 0 && fl) atomicOr(&A.t_flags[t], fl);
+    __syncthreads();
+  }
+}
+
+// gamma(lambda) of the current state into the per-cell gamma buffer.
+template <typename R>
+__global__ void gamma_kernel(StepArgs A) {
+  for (int i = blockIdx.y; i < A.ninst; i += gridDim.y) {
+    const InstDesc& d = A.desc[i];
+    const InstState& st = A.st[i];
+    if (!d.var_gamma || !d.gam) continue;
+    const R* lam = (const R*)d.lam[(st.cur + A.src_off) % d.nring];
+    R* gam = (R*)d.gam;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < d.ncell;
+         k += (int64_t)gridDim.x * blockDim.x)
+      gam[k] = gamma_of_lambda(lam[k]);
+  }
 }
 
 #ifdef TFV_DEFINE_SHARED_KERNELS  // defined by exactly one translation unit
@@ -1163,6 +1449,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(StepArgs A, int mode, int
   const InstDesc& d = A.desc[i];
   InstState& st = A.st[i];
   if (mode == 0 && st.status != kReady) return;  // uniform
+  if (mode == 4 && st.status != kReady && st.status != kRetry) return;
   const int nv = d.dim + 2;
   int fl = 0;
   double w[3] = {0.0, 0.0, 0.0};
@@ -1174,7 +1461,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(StepArgs A, int mode, int
     for (int k = 0; k < 3; ++k) w[k] = fmax(w[k], A.t_wmax[(size_t)t * 3 + k]);
     if (mode == 0)
       for (int k = 0; k < 15; ++k) s[k] += A.t_bsum[(size_t)t * 15 + k];
-    if (mode >= 2)
+    if (mode == 2 || mode == 3 || (mode == 0 && d.reactive))
       for (int k = 0; k < 5; ++k) isum[k] += A.t_sum[(size_t)t * 5 + k];
   }
   fl = block_or(fl, reinterpret_cast<int*>(red));
@@ -1189,7 +1476,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(StepArgs A, int mode, int
       if (threadIdx.x == 0) sh_s[k] = v;
     }
   }
-  if (mode >= 2) {
+  if (mode == 2 || mode == 3 || (mode == 0 && d.reactive)) {
     for (int k = 0; k < 5; ++k) {
       const double v = block_sum(isum[k], red);
       if (threadIdx.x == 0) sh_i[k] = v;
@@ -1203,6 +1490,28 @@ __global__ void __launch_bounds__(256) finalize_kernel(StepArgs A, int mode, int
   if (mode == 3) {
     for (int c = 0; c < 5; ++c) st.initial[c] = c < nv ? sh_i[c] * d.vol : 0.0;
   }
+  if (mode == 4) {
+    if (sh_f & kFlagChemistry) {
+      st.status = kErrChemistry;
+      return;
+    }
+    const double allowed = cfl_dt(d, sh_w);
+    double dt = st.dt;
+    if (dt <= allowed * (1 + 1e-12)) {
+      st.status = kReady;
+      return;
+    }
+    st.retry += 1;
+    if (st.retry >= 60) {
+      st.status = kErrReactive;
+      return;
+    }
+    dt = (dt / 2 <= allowed) ? dt / 2 : allowed;
+    if (fp32) dt = (double)(float)dt;
+    set_dt(d, st, dt);
+    st.status = kRetry;
+    return;
+  }
   if (mode == 0) {
     if (sh_f & kFlagNonphysical) {
       st.status = kErrNonphysical;
@@ -1214,11 +1523,17 @@ __global__ void __launch_bounds__(256) finalize_kernel(StepArgs A, int mode, int
       st.fb_word = 0;
       return;
     }
+    if (sh_f & kFlagChemistry) {
+      st.status = kErrChemistry;
+      st.fb_word = 0;
+      return;
+    }
     const double dt = st.dt;
     for (int c = 0; c < nv; ++c) {
       double out = 0.0;
       for (int k = 0; k < d.dim; ++k) out += dt * d.vol / d.h[k] * sh_s[k * 5 + c];
       st.boundary[c] += out;
+      if (d.reactive) st.source[c] += d.vol * sh_i[c];
     }
     st.cur = (st.cur + A.dst_off) % d.nring;
     const double tn = st.time + dt;

@@ -9,7 +9,8 @@
 
 namespace tfv {
 
-enum : int { kOpHydro = 0, kOpFallback = 1, kOpWaves = 2 };
+enum : int { kOpHydro = 0, kOpFallback = 1, kOpWaves = 2, kOpReact1 = 3, kOpReact2 = 4,
+             kOpSpecies = 5, kOpGamma = 6 };
 
 // lim selects the limiter instantiation of the step kernel (ignored otherwise).
 cudaError_t launch_step2_f64(int op, bool varg, int lim, const StepArgs& A, int grid, int block,

@@ -21,6 +21,7 @@ struct InstDesc {
   int32_t controller, variant, wavespeed;  // 1D options
   int32_t tile0, ntiles; // range of this instance in the tile table
   int32_t has_flux_out;
+  int32_t flux_nv;       // components written to flux_out (all for return_fluxes, 1 = mass)
   int32_t tma;           // tensor maps of this instance's buffers are valid
   int64_t ncell;
   int64_t max_steps;

@@ -91,7 +91,8 @@ def _dtype(precision):
 class _Engine:
     """One batch handle with its device memory (ring buffers and workspace)."""
 
-    def __init__(self, dim, precision, cfgs, states, device, tile=None, stream=None):
+    def __init__(self, dim, precision, cfgs, states, device, tile=None, stream=None, lams=None,
+                 betas=None):
         lib = _lib.load()
         self.lib = lib
         self.dim = dim
@@ -120,19 +121,22 @@ class _Engine:
         self.workspace = torch.empty(ws.value + 256, dtype=torch.uint8, device=device)
         off = (-self.workspace.data_ptr()) % 256
         self.ws_ptr = self.workspace.data_ptr() + off
-        self.rings = []
-        ptrs = []
-        with torch.cuda.stream(self.stream):
-            for s in states:
-                ring = [torch.as_tensor(s, dtype=self.dtype).to(device, non_blocking=False)]
-                ring[0] = ring[0].contiguous()
+        def make_rings(arrays):
+            rings, ptrs = [], []
+            for a in arrays:
+                ring = [torch.as_tensor(np.asarray(a), dtype=self.dtype).to(device).contiguous()]
                 for _ in range(self.nring - 1):
                     ring.append(torch.empty_like(ring[0]))
-                self.rings.append(ring)
+                rings.append(ring)
                 ptrs.extend(r.data_ptr() for r in ring)
+            return rings, (C.c_void_p * len(ptrs))(*ptrs) if ptrs else None
+
+        with torch.cuda.stream(self.stream):
+            self.rings, parr = make_rings(states)
+            self.lam_rings, larr = make_rings(lams) if lams is not None else ([], None)
+            self.beta_rings, barr = make_rings(betas) if betas is not None else ([], None)
         self.stream.synchronize()
-        parr = (C.c_void_p * len(ptrs))(*ptrs)
-        _lib.check(lib.tfv_batch_bind(handle, C.c_void_p(self.ws_ptr), parr, None, None,
+        _lib.check(lib.tfv_batch_bind(handle, C.c_void_p(self.ws_ptr), parr, larr, barr,
                                       _lib.stream_ptr(self.stream)))
         self.reports = (_lib.Report * self.n)()
         self.refresh()
@@ -160,6 +164,12 @@ class _Engine:
 
     def current(self, i=0):
         return self.rings[i][self.reports[i].current]
+
+    def current_lam(self, i=0):
+        return self.lam_rings[i][self.reports[i].current] if self.lam_rings else None
+
+    def current_beta(self, i=0):
+        return self.beta_rings[i][self.reports[i].current] if self.beta_rings else None
 
     def replan(self):
         _lib.check(self.lib.tfv_batch_replan(self.handle))
@@ -225,15 +235,14 @@ class Simulation:
         self._validate_config()
         if not np.isfinite(primitive).all() or np.any(primitive[[0, -1]] <= 0):
             raise ValueError("Initial density and pressure must be positive and primitives finite")
-        if reactive:
-            raise NotImplementedError("reactive sessions are not available in this build yet")
-        if lambda_init is not None or beta_init is not None:
-            raise ValueError("Composition requires reactive chemistry; beta requires ZND")
         if dim == 1:
             raise NotImplementedError("1D sessions are not available in this build yet")
-        self.lam = None
-        self.beta = None
-        g = self.gamma
+        lam0 = self._fraction(lambda_init, "lambda") if reactive else None
+        beta0 = self._fraction(beta_init, "beta") if reactive and kinetic_model == "znd" else None
+        if (not reactive and lambda_init is not None) or (beta_init is not None and beta0 is None):
+            raise ValueError("Composition requires reactive chemistry; beta requires ZND")
+        self._lam0 = lam0
+        g = self._gamma_of(lam0)
         state = prim_to_cons(primitive, g)
         if not _physical(state):
             raise ValueError("Nonphysical initial conservative state")
@@ -245,12 +254,28 @@ class Simulation:
                           kinetic_model=kinetic_model, closure=closure, chemistry=chem,
                           inlet_primitive=inlet_primitive, controller=controller,
                           variant=variant, wavespeed=wavespeed)
-        self._engine = _Engine(dim, precision, [cfg], [state], self.device, tile=tile)
+        self._engine = _Engine(dim, precision, [cfg], [state], self.device, tile=tile,
+                               lams=None if lam0 is None else [lam0],
+                               betas=None if beta0 is None else [beta0])
         if graph_steps:
             self._engine.use_graph(graph_steps)
         self.run_id = str(uuid.uuid4())
         self._workers = 1
         self.set_workers(workers)
+
+    def _fraction(self, values, name):
+        """Composition arrays (torchSession.py:256-271)."""
+        shape = tuple(self.config["counts_xyz"][::-1])
+        result = np.ones(shape) if values is None else np.array(values, dtype=float, copy=True)
+        if (result.shape != shape or not np.isfinite(result).all()
+                or np.any((result < 0) | (result > 1))):
+            raise ValueError(f"{name} must have the spatial shape and values in [0,1]")
+        return result
+
+    def _gamma_of(self, lam):
+        if self.config["reactive"] and self._closure == "si" and lam is not None:
+            return (4.5 - lam) / (3.5 - lam)
+        return self.config["gamma"]
 
     # -- validation (torchSession.py:190-254) -------------------------------
     def _validate_config(self):
@@ -351,9 +376,22 @@ class Simulation:
 
     @property
     def gamma(self):
-        if self.config["reactive"] and self._closure == "si" and self.lam is not None:
-            return (4.5 - self.lam) / (3.5 - self.lam)
-        return self.config["gamma"]
+        return self._gamma_of(self.lam)
+
+    @property
+    def lam(self):
+        if not self.config["reactive"]:
+            return None
+        self._engine.stream.synchronize()
+        return self._engine.current_lam().detach().to("cpu", torch.float64).numpy()
+
+    @property
+    def beta(self):
+        t = self._engine.current_beta()
+        if t is None:
+            return None
+        self._engine.stream.synchronize()
+        return t.detach().to("cpu", torch.float64).numpy()
 
     @property
     def spacing(self):
@@ -387,8 +425,10 @@ class Simulation:
     # -- stepping ------------------------------------------------------------
     def _raise_pending(self):
         status = self._report.status
-        if status in (_lib.READY, _lib.DONE):
+        if status in (_lib.READY, _lib.DONE, _lib.RETRY):
             return
+        if status == _lib.ERR_CHEMISTRY:  # the reference's reaction step raises ValueError
+            raise ValueError(_lib.STATUS_MESSAGES[status])
         raise RuntimeError(_lib.STATUS_MESSAGES.get(status, _lib.STATUS[status]))
 
     def step(self):
@@ -397,8 +437,11 @@ class Simulation:
             return
         self._raise_pending()  # max steps / stall found when this step was planned
         before = self.steps
-        self._engine.advance(1)
-        self._engine.refresh()
+        for _ in range(61):  # a reactive step may take up to 60 dt halvings
+            self._engine.advance(1)
+            self._engine.refresh()
+            if self._report.status != _lib.RETRY:
+                break
         if self.steps == before:
             self._raise_pending()  # the step itself failed; nothing was committed
 
