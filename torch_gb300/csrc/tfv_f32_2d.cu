@@ -5,4 +5,6 @@
 #define TFV_WITH_2D 1
 #define TFV_WITH_3D 0
 #define TFV_LAUNCH2_NAME launch_step2_f32
+#define TFV_WITH_1D 1
+#define TFV_LAUNCH1_NAME launch_step1_f32
 #include "tfv_inst.inc"

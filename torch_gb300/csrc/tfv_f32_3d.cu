@@ -9,4 +9,5 @@
 #define TFV_WITH_3D 1
 #define TFV_LAUNCH3_NAME launch_step3_f32
 #define TFV_HLLC_NAME launch_hllc_f32
+#define TFV_WITH_1D 0
 #include "tfv_inst.inc"

@@ -10,6 +10,8 @@
 #define TFV_LAUNCH2_NAME launch_step2_f64
 #define TFV_LAUNCH3_NAME launch_step3_f64
 #define TFV_HLLC_NAME launch_hllc_f64
+#define TFV_WITH_1D 1
+#define TFV_LAUNCH1_NAME launch_step1_f64
 #include "tfv_inst.inc"
 
 namespace tfv {

@@ -65,7 +65,7 @@ struct tfv_batch {
          off_flags = 0, off_int = 0, off_gam = 0, off_tmaps = 0, total = 0;
   std::vector<CUtensorMap> tmaps;  // [n][4]: ring buffers 0..2, gamma
   size_t gam_bytes = 0;
-  size_t off_mflux = 0, mflux_bytes = 0;
+  size_t off_mflux = 0, mflux_bytes = 0, off_scratch = 0;
   unsigned char* ws = nullptr;
   cudaStream_t stream = nullptr;
   StepArgs args{};
@@ -212,7 +212,7 @@ void layout(tfv_batch* b) {
   o = align_up(o, 256);
   b->off_mflux = o;
   b->mflux_bytes = 0;
-  if (b->reactive) {  // face mass fluxes of the hydro step, read by the species transport
+  if (b->reactive && b->dim > 1) {  // face mass fluxes of the hydro step, read by the species transport
     for (int i = 0; i < b->n; ++i) {
       const InstDesc& d = b->desc[i];
       for (int k = 0; k < b->dim; ++k)
@@ -220,6 +220,10 @@ void layout(tfv_batch* b) {
     }
   }
   o += b->mflux_bytes;
+  o = align_up(o, 256);
+  b->off_scratch = o;  // 1D: waves [3][n+1], reconstruction [6][n], fluxes [3][n+1]
+  if (b->dim == 1)
+    for (int i = 0; i < b->n; ++i) o += align_up(real_size(b->precision) * (12 * b->desc[i].ncell + 6), 256);
   b->total = align_up(o, 256);
 }
 
@@ -287,9 +291,12 @@ cudaError_t launch_range(tfv_batch* b, int op, int lim, int t0, int t1, int src_
   A.t_begin = t0;
   A.t_end = t1;
   const int grid = grid_for(b, t1 - t0);
-  if (b->precision == TFV_FP64)
+  if (b->precision == TFV_FP64) {
+    if (b->dim == 1) return launch_step1_f64(op, b->varg, lim, A, grid, b->block, b->stream);
     return b->dim == 3 ? launch_step3_f64(op, b->varg, lim, A, grid, b->block, b->stream)
                        : launch_step2_f64(op, b->varg, lim, A, grid, b->block, b->stream);
+  }
+  if (b->dim == 1) return launch_step1_f32(op, b->varg, lim, A, grid, b->block, b->stream);
   return b->dim == 3 ? launch_step3_f32(op, b->varg, lim, A, grid, b->block, b->stream)
                      : launch_step2_f32(op, b->varg, lim, A, grid, b->block, b->stream);
 }
@@ -321,6 +328,24 @@ cudaError_t finalize(tfv_batch* b, int mode, int dst_off) {
 // species transport; second half reaction (cur+2 -> cur+1) with the source
 // sums; commit (cur <- cur+1).
 cudaError_t enqueue_step(tfv_batch* b) {
+  if (b->dim == 1) {  // the 1D chain: wave speeds of the new state plan the next dt
+    cudaError_t e = cudaSuccess;
+    if (b->reactive) {
+      e = launch(b, kOpReact1, 0, 1);
+      if (e == cudaSuccess) e = launch(b, kOpWaves, 1, 1);
+      if (e == cudaSuccess) e = finalize(b, 4, 1);
+      if (e == cudaSuccess) e = launch(b, kOpHydro, 1, 2);
+      if (e == cudaSuccess) e = launch(b, kOpFallback, 1, 2);
+      if (e == cudaSuccess) e = launch(b, kOpSpecies, 1, 2);
+      if (e == cudaSuccess) e = launch(b, kOpReact2, 2, 1);
+    } else {
+      e = launch(b, kOpHydro, 0, 1);
+      if (e == cudaSuccess) e = launch(b, kOpFallback, 0, 1);
+    }
+    if (e == cudaSuccess) e = launch(b, kOpWaves, 1, 1);
+    if (e == cudaSuccess) e = finalize(b, 0, 1);
+    return e;
+  }
   if (b->reactive) {
     cudaError_t e = launch(b, kOpReact1, 0, 1);
     if (e == cudaSuccess) e = finalize(b, 4, 1);
@@ -363,7 +388,7 @@ int tfv_batch_create(int32_t dim, int32_t precision, int32_t n, const tfv_config
 static int create_internal(int32_t dim, int32_t precision, int32_t n, const tfv_config* cfgs,
                            const tfv_tile* tile, bool varg, tfv_batch** out) {
   if (!out || !cfgs || n < 1) return fail(TFV_EINVAL, "invalid arguments");
-  if (dim != 2 && dim != 3) return fail(TFV_EINVAL, "dimension must be 2 or 3 for a batch");
+  if (dim < 1 || dim > 3) return fail(TFV_EINVAL, "dimension must be 1, 2 or 3");
   if (precision != TFV_FP64 && precision != TFV_FP32) return fail(TFV_EINVAL, "bad precision");
   for (int i = 0; i < n; ++i) {
     const int r = validate(cfgs[i], dim);
@@ -390,7 +415,7 @@ static int create_internal(int32_t dim, int32_t precision, int32_t n, const tfv_
   if (tile) {
     b->tile = *tile;
   } else {
-    b->tile.tx = dim == 3 ? 32 : 128;
+    b->tile.tx = dim == 3 ? 32 : (dim == 2 ? 128 : 256);
     b->tile.ty = dim == 3 ? (precision == TFV_FP64 ? 4 : 8) : 1;
     b->tile.chunk = dim == 3 ? 32 : 32;
     b->tile.persistent_ctas = 0;
@@ -470,7 +495,16 @@ int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* con
         d.gam = b->ws + og;
         og += align_up(real_size(b->precision) * d.ncell, 256);
       }
-      if (b->reactive) {
+      if (b->dim == 1) {  // the 1D scratch; its flux rows feed the species transport
+        size_t off = b->off_scratch;
+        for (int j = 0; j < i; ++j)
+          off += align_up(real_size(b->precision) * (12 * b->desc[j].ncell + 6), 256);
+        d.scratch = b->ws + off;
+        d.flux_out[0] = static_cast<unsigned char*>(d.scratch) +
+                        real_size(b->precision) * (3 * (d.ncell + 1) + 6 * d.ncell);
+        d.flux_out[1] = d.flux_out[2] = nullptr;
+        d.has_flux_out = 0;
+      } else if (b->reactive) {
         for (int k = 0; k < 3; ++k) d.flux_out[k] = nullptr;
         for (int k = 0; k < b->dim; ++k) {
           d.flux_out[k] = b->ws + om;
@@ -484,7 +518,7 @@ int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* con
   b->tmaps.assign((size_t)b->n * 4, CUtensorMap{});
   for (int i = 0; i < b->n; ++i) {
     InstDesc& d = b->desc[i];
-    bool ok = b->tile.tma != 0;
+    bool ok = b->tile.tma != 0 && b->dim > 1;
     for (int k = 0; k < b->nring && ok; ++k) ok = encode_map(&b->tmaps[i * 4 + k], b, d, d.U[k], false);
     if (ok && b->varg) ok = encode_map(&b->tmaps[i * 4 + 3], b, d, d.gam, true);
     d.tma = ok ? 1 : 0;

@@ -187,10 +187,10 @@ struct Geo {
   __device__ __forceinline__ void init(const InstDesc& d) {
     na = d.n[0];
     nb = DIM == 3 ? d.n[1] : 1;
-    np = d.n[DIM - 1];
+    np = DIM == 1 ? 1 : d.n[DIM - 1];  // a 1D grid is a single row
     bca = d.bc[0];
     bcb = DIM == 3 ? d.bc[1] : kBcOpen;
-    bcp = d.bc[DIM - 1];
+    bcp = DIM == 1 ? kBcOpen : d.bc[DIM - 1];
     ps = (int64_t)na * nb;
     cs = ps * np;
   }
@@ -466,6 +466,12 @@ __device__ __forceinline__ void wave_speeds(const R* u, R g, R* w) {
 #pragma unroll
       for (int k = 0; k < 3; ++k) w[k] = fabs(u[k + 1] * irho) + a;
     }
+  } else if (DIM == 1) {
+    // hydro_dt_1d: uconsv_to_uprim + sound_speed_calc (pressure floored at 0)
+    const R rho = np_max(u[0], R(kFloor));
+    const R v = u[1] / rho;
+    const R p = np_max((u[2] - (R(0.5) * rho) * (v * v)) * (g - R(1)), R(kFloor));
+    w[0] = fabs(v) + sqrt((g * np_max(p, R(0))) / np_max(rho, R(kFloor)));
   } else {
     const R rho = np_max(u[0], R(kFloor));
     const R vx = u[1] / rho;
@@ -1211,9 +1217,12 @@ __device__ __forceinline__ bool react_cell(const InstDesc& d, R* u, R& lam, R& b
                                            double dt_r) {
   constexpr int NV = DIM + 2;
   const R s0 = u[0], s1 = u[1];
-  R st = u[2] * u[2];
-  if (DIM == 3) st = st + u[3] * u[3];
-  const R s2 = u[NV - 1] - (R(0.5) * st) / u[0];
+  R s2 = u[NV - 1];  // 1D: the state itself (torchSession.py:365-369)
+  if (DIM > 1) {     // 2D/3D: move the transverse kinetic energy out of E
+    R st = u[2] * u[2];
+    if (DIM == 3) st = st + u[3] * u[3];
+    s2 = u[NV - 1] - (R(0.5) * st) / u[0];
+  }
   bool ok = finite_(lam) && lam >= R(0) && lam <= R(1);
   const R e1 = s2 - (R(0.5) * (s1 * s1)) / s0;
   ok = ok && finite_(s0) && finite_(s1) && finite_(s2) && s0 > R(kFloor) && e1 > R(kFloor);
@@ -1238,7 +1247,7 @@ __device__ __forceinline__ bool react_cell(const InstDesc& d, R* u, R& lam, R& b
   R lam_new, beta_new;
   advance(reaction_rate<R>(d, lam_mid, s0, s1, s2_mid), R(dt_r), lam_new, beta_new);
   const R s2_new = s2 + (q * s0) * (lam_n - lam_new);
-  u[NV - 1] = u[NV - 1] + (s2_new - s2);
+  u[NV - 1] = DIM == 1 ? s2_new : u[NV - 1] + (s2_new - s2);
   lam = lam_new;
   if (znd) beta = beta_new;
   return ok;
@@ -1391,7 +1400,7 @@ __global__ void __launch_bounds__(256) species_kernel(StepArgs A) {
           for (int dd = 0; dd < DIM; ++dd) {
             const int ia = dd == 0 ? 1 : 0;
             const int ib = (DIM == 3 && dd == 1) ? 1 : 0;
-            const int ip = dd == DIM - 1 ? 1 : 0;
+            const int ip = (DIM > 1 && dd == DIM - 1) ? 1 : 0;  // 1D has no marching axis
             // face arrays of this direction have one more entry along dd
             const int fa_n = dd == 0 ? g.na + 1 : g.na;
             const int fb_n = (DIM == 3 && dd == 1) ? g.nb + 1 : g.nb;

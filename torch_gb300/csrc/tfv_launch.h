@@ -13,6 +13,10 @@ enum : int { kOpHydro = 0, kOpFallback = 1, kOpWaves = 2, kOpReact1 = 3, kOpReac
              kOpSpecies = 5, kOpGamma = 6 };
 
 // lim selects the limiter instantiation of the step kernel (ignored otherwise).
+cudaError_t launch_step1_f64(int op, bool varg, int lim, const StepArgs& A, int grid, int block,
+                             cudaStream_t s);
+cudaError_t launch_step1_f32(int op, bool varg, int lim, const StepArgs& A, int grid, int block,
+                             cudaStream_t s);
 cudaError_t launch_step2_f64(int op, bool varg, int lim, const StepArgs& A, int grid, int block,
                              cudaStream_t s);
 cudaError_t launch_step3_f64(int op, bool varg, int lim, const StepArgs& A, int grid, int block,

@@ -235,8 +235,6 @@ class Simulation:
         self._validate_config()
         if not np.isfinite(primitive).all() or np.any(primitive[[0, -1]] <= 0):
             raise ValueError("Initial density and pressure must be positive and primitives finite")
-        if dim == 1:
-            raise NotImplementedError("1D sessions are not available in this build yet")
         lam0 = self._fraction(lambda_init, "lambda") if reactive else None
         beta0 = self._fraction(beta_init, "beta") if reactive and kinetic_model == "znd" else None
         if (not reactive and lambda_init is not None) or (beta_init is not None and beta0 is None):
