@@ -170,6 +170,14 @@ int tfv_batch_report(tfv_batch* b, tfv_report* out);
  * (python/cfdSolver/torchSession.py:285-295). */
 int tfv_batch_integrals(tfv_batch* b, double* out);
 
+/* Carry instances that already advanced into this (freshly bound) batch:
+ * for each i with reports[i].steps > 0 or reports[i].time > 0, restore time,
+ * steps, integrals, fallback counters and a terminal status, then re-plan dt
+ * from the current states.  The caller passes each instance's current state
+ * as ring buffer 0 at bind.  Used to re-batch grids when requests join or
+ * leave (no reference counterpart: TORCH sessions are never batched). */
+int tfv_batch_restore(tfv_batch* b, const tfv_report* reports);
+
 /* Re-plan after the caller wrote new values into the current buffers
  * (recomputes dt and status; keeps time, steps and integrals). */
 int tfv_batch_replan(tfv_batch* b);

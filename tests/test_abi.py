@@ -62,3 +62,23 @@ def test_invalid_arguments_are_rejected_without_a_gpu():
     assert "cells" in _lib.last_error()
     with pytest.raises(ValueError):
         _lib.check(code)
+
+
+def _weak_symbols(obj):
+    out = subprocess.run(["nm", "--defined-only", str(obj)], capture_output=True, text=True,
+                         check=True).stdout
+    return {line.split()[-1] for line in out.splitlines()
+            if len(line.split()) == 3 and line.split()[1] in ("W", "V") and "3tfv" in line}
+
+
+def test_precision_units_share_no_mergeable_symbols():
+    """The double and single precision units compile the same sources with a
+    different REAL.  A weak (mergeable) tfv symbol defined in both would be
+    linked once and run one precision's kernels on the other's buffers."""
+    from torch_gb300 import build
+    build.build()
+    objs = {name: build.BUILD / (Path(name).stem + ".o") for name in build.UNITS}
+    f64 = _weak_symbols(objs["tfv_f64.cu"])
+    for unit in ("tfv_f32_2d.cu", "tfv_f32_3d.cu"):
+        shared = f64 & _weak_symbols(objs[unit])
+        assert not shared, sorted(shared)[:5]

@@ -110,3 +110,23 @@ def test_1d_fallback_matches_oracle():
         assert gpu.fallback_steps == ref.fallback_steps
         seen += ref.fallback_steps
     assert seen > 0
+
+
+def test_1d_many_tiles_fp64_bitwise_and_fp32_close():
+    """3001 cells span twelve 256-cell tiles.  FP64 stays bit-identical to the
+    oracle; the FP32 chain (its own kernels, not the FP64 ones) stays within
+    an L1 density error of 1e-5 of FP64."""
+    p = sod(3001, left=(1.0, 0.0, 1.0), right=(0.125, 0.0, 0.1))
+    kw = dict(t_end=0.2, limiter="MINBEE")
+    ref = OracleSimulation(p, [1.0], **kw)
+    s64 = torch_gb300.Simulation(p, [1.0], **kw)
+    s32 = torch_gb300.Simulation(p, [1.0], precision="fp32", **kw)
+    for _ in range(10):
+        ref.step()
+        s64.step()
+    np.testing.assert_array_equal(s64.state, ref.state)
+    s64.run(step_limit=200)
+    s32.run(step_limit=210)
+    assert s32.steps == s64.steps == 210
+    assert np.mean(np.abs(s32.state[0] - s64.state[0])) <= 1e-5
+    assert np.max(np.abs(s32.balance_residual) / np.abs(s32.initial_integral).max()) < 1e-6

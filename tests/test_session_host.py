@@ -54,3 +54,21 @@ def test_conversion_matches_oracle_bitwise():
     p = 0.5 + rng.random((5, 3, 4, 5))
     np.testing.assert_array_equal(prim_to_cons(p, 1.4), fv.prim_to_cons(p, 1.4))
     assert _physical(prim_to_cons(p, 1.4)) == fv.physical(fv.prim_to_cons(p, 1.4))
+
+
+def test_served_request_stream_mix_and_determinism():
+    from torch_gb300.serve import served_requests
+
+    a = served_requests(rate=100.0, count=400, seed=7)
+    b = served_requests(rate=100.0, count=400, seed=7)
+    assert [(r.dim, r.n, r.arrival) for r in a] == [(r.dim, r.n, r.arrival) for r in b]
+    dims = np.array([r.dim for r in a])
+    assert abs(np.mean(dims == 1) - 0.4) < 0.08 and abs(np.mean(dims == 3) - 0.2) < 0.06
+    assert all(1e3 <= r.n <= 1e5 for r in a if r.dim == 1)
+    assert all(128 <= r.n <= 1024 for r in a if r.dim == 2)
+    assert all(64 <= r.n <= 256 for r in a if r.dim == 3)
+    assert all(0.1 <= r.t_end <= 0.3 for r in a)
+    gaps = np.diff([0.0] + [r.arrival for r in a])
+    assert abs(gaps.mean() - 0.01) < 0.002  # Poisson at 100 requests/s
+    p = a[0].primitive()
+    assert p.shape[0] == a[0].dim + 2 and np.all(p[0] > 0) and np.all(p[-1] > 0)

@@ -77,6 +77,7 @@ _SIGS = {
     "tfv_batch_report": ([_VP, C.POINTER(Report)], C.c_int),
     "tfv_batch_integrals": ([_VP, C.POINTER(C.c_double)], C.c_int),
     "tfv_batch_replan": ([_VP], C.c_int),
+    "tfv_batch_restore": ([_VP, C.POINTER(Report)], C.c_int),
     "tfv_batch_set_flux_outputs": ([_VP, C.c_int32, _VP, _VP, _VP], C.c_int),
     "tfv_batch_destroy": ([_VP], C.c_int),
     "tfv_batch_profile": ([_VP, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float),
@@ -92,8 +93,13 @@ _SIGS = {
 _lib = None
 
 
+def checked():
+    """TORCH_GB300_CHECKED=1 selects the checked build of the library."""
+    return os.environ.get("TORCH_GB300_CHECKED", "0") not in ("", "0")
+
+
 def library_path():
-    return _build.LIB
+    return _build.library(checked())
 
 
 def load(build_if_missing=True):
@@ -101,9 +107,9 @@ def load(build_if_missing=True):
     global _lib
     if _lib is not None:
         return _lib
-    path = _build.LIB
+    path = library_path()
     if build_if_missing and (not path.exists() or _build._sources_newer(path)):
-        _build.build()
+        _build.build(checked=checked())
     if not path.exists():
         raise RuntimeError(f"libtfv.so is missing at {path}; run python -m torch_gb300.build")
     lib = C.CDLL(os.fspath(path))

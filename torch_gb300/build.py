@@ -5,7 +5,9 @@
 Each translation unit is compiled by nvcc in parallel; the double-precision
 kernels are built with -fmad=false so that they keep NumPy's rounding, the
 single-precision kernels with FMA contraction, flush-to-zero and fast
-division/square root.  Output: torch_gb300/_build/libtfv.so.
+division/square root.  Output: torch_gb300/_build/libtfv.so; with --checked,
+the checked build torch_gb300/_build/checked/libtfv.so (kernel indexes
+tested against their buffers, for debugging).
 """
 
 import os
@@ -20,6 +22,7 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 BUILD = PKG / "_build"
 LIB = BUILD / "libtfv.so"
+CHECKED_LIB = BUILD / "checked" / "libtfv.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + str(INCLUDE),
@@ -51,17 +54,26 @@ def _sources_newer(target):
     return any(p.stat().st_mtime > t for p in deps)
 
 
-def build(force=False, verbose=False):
+def library(checked=False):
+    """Path of the library: the release build, or the checked build (every
+    kernel index tested against its buffer, each launch waited for)."""
+    return CHECKED_LIB if checked else LIB
+
+
+def build(force=False, verbose=False, checked=False):
     """Compile every unit and link libtfv.so; returns its path."""
-    if not force and not _sources_newer(LIB):
-        return LIB
-    BUILD.mkdir(parents=True, exist_ok=True)
+    lib = library(checked)
+    if not force and not _sources_newer(lib):
+        return lib
+    out = lib.parent
+    out.mkdir(parents=True, exist_ok=True)
     nvcc = nvcc_path()
+    extra = ["-DTFV_CHECKED=1"] if checked else []
 
     def compile_unit(item):
         src, flags = item
-        obj = BUILD / (Path(src).stem + ".o")
-        cmd = [nvcc, *ARCH, *COMMON, *flags, "-c", str(CSRC / src), "-o", str(obj)]
+        obj = out / (Path(src).stem + ".o")
+        cmd = [nvcc, *ARCH, *COMMON, *extra, *flags, "-c", str(CSRC / src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd), flush=True)
         res = subprocess.run(cmd, capture_output=True, text=True)
@@ -71,14 +83,14 @@ def build(force=False, verbose=False):
 
     with ThreadPoolExecutor(max_workers=len(UNITS)) as pool:
         objs = list(pool.map(compile_unit, UNITS.items()))
-    tmp = BUILD / "libtfv.so.tmp"
+    tmp = out / "libtfv.so.tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart_static"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose=True))
+    print(build(force="--force" in sys.argv, verbose=True, checked="--checked" in sys.argv))

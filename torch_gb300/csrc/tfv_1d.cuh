@@ -41,6 +41,10 @@ __device__ __forceinline__ void cell1(const InstDesc& d, const R* U, int k, R* u
     src = d.bc[0] == kBcPeriodic ? 0 : n - 1;
     flip = d.bc[0] == kBcReflective;
   }
+  if (!TFV_IN(40, src, n)) {
+    u[0] = u[1] = u[2] = R(0);
+    return;
+  }
   u[0] = U[src];
   u[1] = flip ? -U[n + src] : U[n + src];
   u[2] = U[2 * n + src];
@@ -241,7 +245,9 @@ template <typename R, bool VARG>
 __global__ void __launch_bounds__(256) waves1d_kernel(StepArgs A) {
   __shared__ double red[40];
   for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
+    if (!TFV_IN(45, t, A.ntiles)) continue;
     const Tile T = A.tiles[t];
+    if (!TFV_IN(46, T.inst, A.ninst)) continue;
     const InstDesc& d = A.desc[T.inst];
     const InstState& st = A.st[T.inst];
     const int n = d.n[0];
@@ -261,6 +267,8 @@ __global__ void __launch_bounds__(256) waves1d_kernel(StepArgs A) {
         waves1(d, L, Rr, gamma1(d, gam, f - 1), gamma1(d, gam, f), s);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
+          if (!TFV_IN(41, f, n + 1)) continue;
+          if (!TFV_INSIDE(62, S.waves + k * (n + 1) + f, d.scratch, S.flux + 3 * (n + 1))) continue;
           S.waves[k * (n + 1) + f] = s[k];
           ws = fmax(ws, (double)fabs(s[k]));
         }
@@ -295,7 +303,9 @@ __global__ void __launch_bounds__(256) waves1d_kernel(StepArgs A) {
 template <typename R, bool VARG>
 __global__ void __launch_bounds__(256) recon1d_kernel(StepArgs A) {
   for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
+    if (!TFV_IN(45, t, A.ntiles)) continue;
     const Tile T = A.tiles[t];
+    if (!TFV_IN(46, T.inst, A.ninst)) continue;
     const InstDesc& d = A.desc[T.inst];
     const InstState& st = A.st[T.inst];
     if (st.status != kReady) continue;
@@ -346,7 +356,11 @@ __global__ void __launch_bounds__(256) recon1d_kernel(StepArgs A) {
       if (badc)
         for (int c = 0; c < 3; ++c) s[c] = c0[c];
     }
+    if (!TFV_IN(42, i, n)) continue;
     for (int c = 0; c < 3; ++c) {
+      if (!TFV_INSIDE(63, S.recon + (3 + c) * n + i, d.scratch, S.flux + 3 * (n + 1)) ||
+          !TFV_INSIDE(64, S.recon + c * n + i, A.ws_lo, A.ws_hi))
+        continue;
       S.recon[c * n + i] = ol[c];
       S.recon[(3 + c) * n + i] = orr[c];
     }
@@ -365,6 +379,10 @@ __device__ __forceinline__ void face_flux1(const InstDesc& d, const R* U, const 
   const R gl = gamma1(d, gam, f - 1), gr = gamma1(d, gam, f);
   if (!first_order) {
     R L[3], Rr[3];
+    if (!TFV_IN(43, f, n + 1)) {
+      F[0] = F[1] = F[2] = R(0);
+      return;
+    }
     face_states1(d, S.recon, f, L, Rr);
     hllc1(d, L, Rr, gl, gr, S.waves[f], S.waves[2 * (n + 1) + f], F);
     return;
@@ -386,7 +404,9 @@ template <typename R, bool VARG>
 __global__ void __launch_bounds__(256) update1d_kernel(StepArgs A, int first_order) {
   __shared__ double red[40];
   for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
+    if (!TFV_IN(45, t, A.ntiles)) continue;
     const Tile T = A.tiles[t];
+    if (!TFV_IN(46, T.inst, A.ninst)) continue;
     const InstDesc& d = A.desc[T.inst];
     InstState& st = A.st[T.inst];
     if (st.status != kReady) continue;
@@ -412,6 +432,10 @@ __global__ void __launch_bounds__(256) update1d_kernel(StepArgs A, int first_ord
       for (int c = 0; c < 3; ++c) un[c] = u[c] + k * (Fp[c] - Fm[c]);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
+        if (!TFV_IN(44, i, n)) continue;
+        if (!TFV_OUTSIDE(65, Un + c * n + i, A.ws_lo, A.ws_hi) ||
+            !TFV_INSIDE(66, S.flux + c * (n + 1) + n, d.scratch, S.flux + 3 * (n + 1)))
+          continue;
         Un[c * n + i] = un[c];
         S.flux[c * (n + 1) + i] = Fm[c];
         if (i == n - 1) S.flux[c * (n + 1) + n] = Fp[c];

@@ -7,4 +7,5 @@
 #define TFV_LAUNCH2_NAME launch_step2_f32
 #define TFV_WITH_1D 1
 #define TFV_LAUNCH1_NAME launch_step1_f32
+#define TFV_CHECK_READ_NAME check_read_f32_2d
 #include "tfv_inst.inc"

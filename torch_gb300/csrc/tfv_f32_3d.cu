@@ -10,4 +10,5 @@
 #define TFV_LAUNCH3_NAME launch_step3_f32
 #define TFV_HLLC_NAME launch_hllc_f32
 #define TFV_WITH_1D 0
+#define TFV_CHECK_READ_NAME check_read_f32_3d
 #include "tfv_inst.inc"

@@ -12,6 +12,7 @@
 #define TFV_HLLC_NAME launch_hllc_f64
 #define TFV_WITH_1D 1
 #define TFV_LAUNCH1_NAME launch_step1_f64
+#define TFV_CHECK_READ_NAME check_read_f64
 #include "tfv_inst.inc"
 
 namespace tfv {

@@ -283,7 +283,106 @@ int grid_for(const tfv_batch* b, int ntiles) {
   return b->tile.persistent_ctas > 0 ? std::min<int>(b->tile.persistent_ctas, ntiles) : ntiles;
 }
 
+#if TFV_CHECKED
+// Checked build: every bound batch is registered; after each launch the whole
+// device is waited for and every registered batch's descriptor and tile table
+// in device memory are compared with the host copies, so that a write into
+// another batch's workspace names the launch that made it.
+std::mutex g_live_mutex;
+std::vector<tfv_batch*> g_live;
+bool g_corrupt = false;  // a registered batch's tables changed: refuse further launches
+
+void live_add(tfv_batch* b) {
+  std::lock_guard<std::mutex> lock(g_live_mutex);
+  g_live.push_back(b);
+}
+void live_remove(tfv_batch* b) {
+  std::lock_guard<std::mutex> lock(g_live_mutex);
+  g_live.erase(std::remove(g_live.begin(), g_live.end(), b), g_live.end());
+}
+
+void integrity(const tfv_batch* by, int op) {
+  std::lock_guard<std::mutex> lock(g_live_mutex);
+  for (tfv_batch* b : g_live) {
+    if (!b->bound || b->ws == nullptr) continue;
+    std::vector<unsigned char> dev(sizeof(InstDesc) * b->n);
+    if (cudaMemcpy(dev.data(), b->ws + b->off_desc, dev.size(), cudaMemcpyDeviceToHost) !=
+        cudaSuccess)
+      return;
+    const unsigned char* host = reinterpret_cast<const unsigned char*>(b->desc.data());
+    for (size_t k = 0; k < dev.size(); ++k)
+      if (dev[k] != host[k]) {
+        std::fprintf(stderr,
+                     "tfv-checked: descriptor of batch %p (dim %d n %d ws %p) changed at byte %zu "
+                     "after op %d of batch %p (dim %d n %d ws %p)\n",
+                     (void*)b, b->dim, b->n, (void*)b->ws, k, op, (const void*)by, by->dim, by->n,
+                     (void*)by->ws);
+        b->bound = false;  // report once
+        g_corrupt = true;
+        break;
+      }
+    if (!b->bound) continue;
+    std::vector<unsigned char> tdev(sizeof(Tile) * b->tiles.size());
+    if (cudaMemcpy(tdev.data(), b->ws + b->off_tiles, tdev.size(), cudaMemcpyDeviceToHost) !=
+        cudaSuccess)
+      return;
+    if (std::memcmp(tdev.data(), b->tiles.data(), tdev.size()) != 0) {
+      std::fprintf(stderr,
+                   "tfv-checked: tile table of batch %p (dim %d n %d ws %p) changed after op %d of "
+                   "batch %p (dim %d n %d ws %p)\n",
+                   (void*)b, b->dim, b->n, (void*)b->ws, op, (const void*)by, by->dim, by->n,
+                   (void*)by->ws);
+      b->bound = false;
+      g_corrupt = true;
+    }
+  }
+}
+
+// Wait for each launch, report the first index violation the kernels
+// recorded (and a fault, naming the launch that raised it).
+cudaError_t checked_sync(const tfv_batch* b, int op, int lim, int t0, int t1, cudaError_t e) {
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    std::fprintf(stderr, "tfv-checked: fault after op %d lim %d tiles [%d,%d) dim %d prec %d n %d: %s\n",
+                 op, lim, t0, t1, b->dim, b->precision, b->n, cudaGetErrorString(e));
+    return e;
+  }
+  cudaError_t (*readers[3])(unsigned long long*) = {check_read_f64, check_read_f32_3d,
+                                                    check_read_f32_2d};
+  for (auto rd : readers) {
+    unsigned long long rec[4] = {0, 0, 0, 0};
+    e = rd(rec);
+    if (e != cudaSuccess) return e;
+    if (rec[0])
+      std::fprintf(stderr,
+                   "tfv-checked: violation op %d lim %d tiles [%d,%d) dim %d prec %d n %d: site %llu "
+                   "block %llu index %lld extent %lld\n",
+                   op, lim, t0, t1, b->dim, b->precision, b->n, rec[0], rec[1], (long long)rec[2],
+                   (long long)rec[3]);
+  }
+  integrity(b, op);
+  return g_corrupt ? cudaErrorNotPermitted : cudaSuccess;
+}
+#endif
+
+cudaError_t launch_range_unchecked(tfv_batch* b, int op, int lim, int t0, int t1, int src_off,
+                                   int dst_off);
+
 cudaError_t launch_range(tfv_batch* b, int op, int lim, int t0, int t1, int src_off, int dst_off) {
+#if TFV_CHECKED
+  if (g_corrupt) return cudaErrorNotPermitted;
+#endif
+  cudaError_t e = launch_range_unchecked(b, op, lim, t0, t1, src_off, dst_off);
+#if TFV_CHECKED
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(b->stream, &cs);
+  if (cs == cudaStreamCaptureStatusNone) e = checked_sync(b, op, lim, t0, t1, e);
+#endif
+  return e;
+}
+
+cudaError_t launch_range_unchecked(tfv_batch* b, int op, int lim, int t0, int t1, int src_off,
+                                   int dst_off) {
   if (t1 <= t0) return cudaSuccess;
   StepArgs A = b->args;
   A.src_off = src_off;
@@ -314,10 +413,19 @@ cudaError_t launch(tfv_batch* b, int op, int src_off, int dst_off) {
 }
 
 cudaError_t finalize(tfv_batch* b, int mode, int dst_off) {
+#if TFV_CHECKED
+  if (g_corrupt) return cudaErrorNotPermitted;
+#endif
   StepArgs A = b->args;
   A.dst_off = dst_off;
-  return launch_finalize(A, mode, b->precision == TFV_FP32,
-                         reinterpret_cast<double*>(b->ws + b->off_int), b->stream);
+  cudaError_t e = launch_finalize(A, mode, b->precision == TFV_FP32,
+                                  reinterpret_cast<double*>(b->ws + b->off_int), b->stream);
+#if TFV_CHECKED
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(b->stream, &cs);
+  if (cs == cudaStreamCaptureStatusNone) e = checked_sync(b, 100 + mode, 0, 0, b->n, e);
+#endif
+  return e;
 }
 
 // Enqueue one complete step for every READY instance.  Reactive steps
@@ -373,7 +481,13 @@ int check_bound(const tfv_batch* b) {
 
 extern "C" {
 
-const char* tfv_version(void) { return "tfv 0.1 (sm_103a)"; }
+const char* tfv_version(void) {
+#if TFV_CHECKED
+  return "tfv 0.1 (sm_103a, checked)";
+#else
+  return "tfv 0.1 (sm_103a)";
+#endif
+}
 
 const char* tfv_last_error(void) { return g_error.c_str(); }
 
@@ -470,6 +584,32 @@ int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* con
   if (!b || !workspace || !states) return fail(TFV_EINVAL, "invalid arguments");
   if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0)
     return fail(TFV_EINVAL, "workspace must be 256-byte aligned");
+  {
+    // the workspace and every state / composition buffer must be disjoint
+    struct Range {
+      uintptr_t lo, hi;
+    };
+    std::vector<Range> r;
+    const uintptr_t w = reinterpret_cast<uintptr_t>(workspace);
+    r.push_back({w, w + b->total});
+    const size_t rs = real_size(b->precision);
+    for (int i = 0; i < b->n; ++i) {
+      const size_t cells = static_cast<size_t>(b->desc[i].ncell);
+      for (int k = 0; k < b->nring; ++k) {
+        const void* u = states[i * b->nring + k];
+        if (u) r.push_back({reinterpret_cast<uintptr_t>(u),
+                            reinterpret_cast<uintptr_t>(u) + rs * (b->dim + 2) * cells});
+        const void* l = lams ? lams[i * b->nring + k] : nullptr;
+        if (l) r.push_back({reinterpret_cast<uintptr_t>(l), reinterpret_cast<uintptr_t>(l) + rs * cells});
+        const void* e = betas ? betas[i * b->nring + k] : nullptr;
+        if (e) r.push_back({reinterpret_cast<uintptr_t>(e), reinterpret_cast<uintptr_t>(e) + rs * cells});
+      }
+    }
+    std::sort(r.begin(), r.end(), [](const Range& x, const Range& y) { return x.lo < y.lo; });
+    for (size_t k = 1; k < r.size(); ++k)
+      if (r[k].lo < r[k - 1].hi)
+        return fail(TFV_EINVAL, "state, composition and workspace buffers must not overlap");
+  }
   b->ws = static_cast<unsigned char*>(workspace);
   b->stream = static_cast<cudaStream_t>(stream);
   for (int i = 0; i < b->n; ++i) {
@@ -541,6 +681,8 @@ int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* con
   A.t_sum = reinterpret_cast<double*>(b->ws + b->off_sum);
   A.t_flags = reinterpret_cast<int32_t*>(b->ws + b->off_flags);
   A.tmaps = b->ws + b->off_tmaps;
+  A.ws_lo = b->ws;
+  A.ws_hi = b->ws + b->total;
   b->block = b->tile.tx * b->tile.ty;
   b->grid = grid_for(b, A.ntiles);
   TFV_CUDA(cudaMemcpyAsync(b->ws + b->off_desc, b->desc.data(), sizeof(InstDesc) * b->n,
@@ -558,6 +700,16 @@ int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* con
   TFV_CUDA(finalize(b, 3, 0));
   TFV_CUDA(cudaStreamSynchronize(b->stream));
   b->bound = true;
+#if TFV_CHECKED
+  live_remove(b);
+  live_add(b);
+  std::fprintf(stderr, "tfv-checked: bind batch %p dim %d n %d ws [%p, +%zu) stream %p\n", (void*)b,
+               b->dim, b->n, (void*)b->ws, b->total, (void*)b->stream);
+  for (int i = 0; i < b->n; ++i)
+    std::fprintf(stderr, "tfv-checked:   inst %d cells %lld U %p %p %p scratch %p\n", i,
+                 (long long)b->desc[i].ncell, b->desc[i].U[0], b->desc[i].U[1], b->desc[i].U[2],
+                 b->desc[i].scratch);
+#endif
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
@@ -647,6 +799,41 @@ int tfv_batch_replan(tfv_batch* b) {
   return TFV_OK;
 }
 
+int tfv_batch_restore(tfv_batch* b, const tfv_report* reports) {
+  int r = check_bound(b);
+  if (r) return r;
+  if (!reports) return fail(TFV_EINVAL, "invalid arguments");
+  TFV_CUDA(cudaMemcpyAsync(b->st.data(), b->ws + b->off_st, sizeof(InstState) * b->n,
+                           cudaMemcpyDeviceToHost, b->stream));
+  TFV_CUDA(cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < b->n; ++i) {
+    const tfv_report& o = reports[i];
+    if (!(o.steps > 0 || o.time > 0)) continue;
+    InstState& s = b->st[i];
+    s.time = o.time;
+    s.steps = o.steps;
+    for (int c = 0; c < 5; ++c) {
+      s.initial[c] = o.initial_integral[c];
+      s.boundary[c] = o.boundary_integral[c];
+      s.source[c] = o.source_integral[c];
+    }
+    s.fallback_steps = o.fallback_steps;
+    s.last_fallback = o.last_fallback;
+    s.cur = 0;
+    s.fb_word = 0;
+    s.retry = 0;
+    // terminal statuses persist; READY / RETRY are re-planned
+    s.status = (o.status == TFV_READY || o.status == TFV_RETRY) ? TFV_READY : o.status;
+  }
+  TFV_CUDA(cudaMemcpyAsync(b->ws + b->off_st, b->st.data(), sizeof(InstState) * b->n,
+                           cudaMemcpyHostToDevice, b->stream));
+  if (b->own_gamma) TFV_CUDA(launch(b, kOpGamma, 0, 0));
+  TFV_CUDA(launch(b, kOpWaves, 0, 0));
+  TFV_CUDA(finalize(b, 1, 0));
+  TFV_CUDA(cudaStreamSynchronize(b->stream));
+  return TFV_OK;
+}
+
 int tfv_batch_set_flux_outputs(tfv_batch* b, int32_t inst, void* fx, void* fy, void* fz) {
   int r = check_bound(b);
   if (r) return r;
@@ -695,6 +882,9 @@ int tfv_batch_profile(tfv_batch* b, int32_t nsteps, float* ms_step, float* ms_fa
 
 int tfv_batch_destroy(tfv_batch* b) {
   if (!b) return TFV_OK;
+#if TFV_CHECKED
+  live_remove(b);
+#endif
   if (b->graph) cudaGraphExecDestroy(b->graph);
   delete b;
   return TFV_OK;

@@ -48,6 +48,51 @@ __device__ __forceinline__ int map_axis(int i, int n, int bc, bool& ghost) {
 }
 
 // --------------------------------------------------------------------------
+// Checked build (TFV_CHECKED=1): every global and shared index of the step
+// kernels is tested against the extent of its buffer; the first violation is
+// recorded (site, block, index, extent) and the access is skipped.  The
+// record is per translation unit; the host reads it after each launch.
+// --------------------------------------------------------------------------
+#if TFV_CHECKED
+static __device__ unsigned long long g_check[4];
+static __device__ __noinline__ void check_fail(int site, long long idx, long long lim) {
+  if (atomicCAS(&g_check[0], 0ull, (unsigned long long)site) == 0ull) {
+    g_check[1] = blockIdx.x;
+    g_check[2] = (unsigned long long)idx;
+    g_check[3] = (unsigned long long)lim;
+  }
+}
+static __device__ __forceinline__ bool in_range(int site, long long idx, long long lim) {
+  if (idx >= 0 && idx < lim) return true;
+  check_fail(site, idx, lim);
+  return false;
+}
+#define TFV_IN(site, idx, lim) ::tfv::in_range((site), (long long)(idx), (long long)(lim))
+// address checks: a state store must lie outside the workspace, a scratch
+// store inside [lo, hi)
+static __device__ __forceinline__ bool outside(int site, const void* p, const void* lo,
+                                               const void* hi) {
+  const char* c = (const char*)p;
+  if (c < (const char*)lo || c >= (const char*)hi) return true;
+  check_fail(site, (long long)(c - (const char*)lo), (long long)((const char*)hi - (const char*)lo));
+  return false;
+}
+static __device__ __forceinline__ bool inside(int site, const void* p, const void* lo,
+                                              const void* hi) {
+  const char* c = (const char*)p;
+  if (c >= (const char*)lo && c < (const char*)hi) return true;
+  check_fail(site, (long long)(c - (const char*)lo), (long long)((const char*)hi - (const char*)lo));
+  return false;
+}
+#define TFV_OUTSIDE(site, p, lo, hi) ::tfv::outside((site), (p), (lo), (hi))
+#define TFV_INSIDE(site, p, lo, hi) ::tfv::inside((site), (p), (lo), (hi))
+#else
+#define TFV_IN(site, idx, lim) true
+#define TFV_OUTSIDE(site, p, lo, hi) true
+#define TFV_INSIDE(site, p, lo, hi) true
+#endif
+
+// --------------------------------------------------------------------------
 // Deterministic block reductions (fixed shuffle tree, warps summed in order).
 // --------------------------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {
@@ -127,6 +172,13 @@ __device__ __forceinline__ void fence_mbar_init() {
 }
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// The tensor maps live in the workspace and are written by host copies
+// between launches; a workspace can reuse the address of an earlier batch's
+// maps.  Acquire each map through the tensormap proxy before its first use
+// so that no stale cached descriptor is used.
+__device__ __forceinline__ void fence_tensormap_acquire(const void* map) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(map) : "memory");
 }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
@@ -209,6 +261,7 @@ __device__ __forceinline__ R fetch_padded(const InstDesc& d, const Geo<DIM>& g, 
     return c < NV ? R(d.inlet[c]) : R(1.4);
   }
   const int64_t off = (int64_t)sp * g.ps + (int64_t)sb * g.na + sa;
+  if (!TFV_IN(1, off, g.cs) || !TFV_IN(2, c, NV + 1)) return R(0);
   if (c == NV) return gam ? gam[off] : R(d.gamma);
   R v = U[c * g.cs + off];
   if ((c == 1 && ga && g.bca == kBcReflective) ||
@@ -296,16 +349,23 @@ struct HydroTile {
         const R* srow = (VARG && c == NV) ? gam + base + (int64_t)lb * g.na
                                           : U + c * g.cs + base + (int64_t)lb * g.na;
         R* drow = dst + c * plane + lb * S.pw + (S.xo - 2);
-        for (int la = lane; la < w; la += 32) drow[la] = srow[la];
+        for (int la = lane; la < w; la += 32) {
+          if (!TFV_IN(3, base + (int64_t)lb * g.na + la, g.cs) ||
+              !TFV_IN(4, c * plane + lb * S.pw + (S.xo - 2) + la, (int64_t)S.slot_elems))
+            continue;
+          drow[la] = srow[la];
+        }
       }
     } else {
       for (int row = threadIdx.x >> 5; row < nrows; row += nwarps) {
         const int c = row / h;
         const int lb = row - c * h;
         R* drow = dst + c * plane + lb * S.pw + (S.xo - 2);
-        for (int la = lane; la < w; la += 32)
+        for (int la = lane; la < w; la += 32) {
+          if (!TFV_IN(5, c * plane + lb * S.pw + (S.xo - 2) + la, (int64_t)S.slot_elems)) continue;
           drow[la] = fetch_padded<R, DIM>(d, g, U, VARG ? gam : (const R*)nullptr, c, x0 - 2 + la,
                                           DIM == 3 ? y0 - 2 + lb : 0, p);
+        }
       }
     }
   }
@@ -342,6 +402,7 @@ struct HydroTile {
         la = aL + (q - row * wm);
         lb = row < bL ? row : (by + 4 - bR) + (row - bL);
       }
+      if (!TFV_IN(6, c * cplane + lb * S.pw + la + (S.xo - 2), (int64_t)S.slot_elems)) continue;
       dst[c * cplane + lb * S.pw + la + (S.xo - 2)] = fetch_padded<R, DIM>(
           d, g, U, VARG ? gam : (const R*)nullptr, c, x0 - 2 + la, DIM == 3 ? y0 - 2 + lb : 0, p);
     }
@@ -366,6 +427,13 @@ __device__ __forceinline__ void cell_stage(const R* ringm, const R* ringc, const
   R* bub = box;                   // predictor
   R* bsa = box + NV * bplane;     // slope along a (x)
   R* bsb = box + 2 * NV * bplane; // slope along b (y), 3D only
+#if TFV_CHECKED
+  if (!TFV_IN(7, li - (DIM == 3 ? S.pw : 0) - 1, plane) ||
+      !TFV_IN(8, li + (DIM == 3 ? S.pw : 0) + 1, plane) || !TFV_IN(9, bi, bplane)) {
+    for (int c = 0; c < NV; ++c) ubar[c] = smarch[c] = R(0);
+    return;
+  }
+#endif
   const R g = VARG ? ringc[NV * plane + li] : gconst;
 
   R u[NV];
@@ -497,7 +565,9 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   constexpr int NV = DIM + 2;
   constexpr int NL = NV + (VARG ? 1 : 0);
   constexpr int MD = DIM - 1;
+  if (!TFV_IN(10, t, A.ntiles)) return true;
   const Tile T = A.tiles[t];
+  if (!TFV_IN(11, T.inst, A.ninst)) return true;
   const InstDesc& d = A.desc[T.inst];
   InstState& st = A.st[T.inst];
   if (st.status != kReady) return true;  // uniform over the CTA
@@ -520,6 +590,10 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   const int x0 = T.x0, y0 = T.y0, p0 = T.p0, p1 = T.p1;
   const int ax = min(S.tx, g.na - x0);
   const int by = DIM == 3 ? min(S.ty, g.nb - y0) : 1;
+  if (!TFV_IN(12, ax - 1, S.tx) || !TFV_IN(13, by - 1, S.ty) || !TFV_IN(14, p0, p1) ||
+      !TFV_IN(15, p1 - 1, g.np) || !TFV_IN(16, blockDim.x - 1, S.tx * S.ty) ||
+      !TFV_IN(17, (int)src, d.nring) || !TFV_IN(18, (int)dst, d.nring))
+    return true;
   const int nint = ax * by;
   const int tid = threadIdx.x;
   const bool owner = tid < nint;
@@ -560,6 +634,10 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   const uint32_t gbox_bytes = VARG ? (uint32_t)(sizeof(R) * S.ph * S.pw) : 0u;
   uint64_t* bars = smem_at<uint64_t>(smem, S.bar_off);
   bool waited_ok = true;
+  if (use_tma && tid == 0) {
+    fence_tensormap_acquire(map_u);
+    if (VARG) fence_tensormap_acquire(map_g);
+  }
   auto stage_begin = [&](int p) {
     R* dst = slot(p);
     if (use_tma && p >= 0 && p < g.np) {
@@ -649,6 +727,7 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
       a = corner_a[q - nring_cells];
       b = corner_b[q - nring_cells];
     }
+    if (!TFV_IN(19, n_ritems, MR)) break;
     items[n_ritems * NT + tid] = ((a + 1) << 15) | (b + 1);
     ++n_ritems;
   }
@@ -665,6 +744,7 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
       const int a = q % ax, bf = q / ax;
       packed = (1 << 30) | ((a + 1) << 15) | (bf + 1);
     }
+    if (!TFV_IN(20, n_fitems, (HydroSmem<R, DIM, VARG>::kMaxFaceItems))) break;
     items[(MR + n_fitems) * NT + tid] = packed;
     ++n_fitems;
   }
@@ -710,6 +790,7 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
         // left cell's box index, step to the right cell, slope array
         const int bl = kind == 0 ? (DIM == 3 ? (j + 1) * S.bw : 0) + i : j * S.bw + i + 1;
         const int br = bl + (kind == 0 ? 1 : S.bw);
+        if (!TFV_IN(21, bl, bplane) || !TFV_IN(22, br, bplane)) continue;
         const R* bsl = box + (kind == 0 ? 1 : 2) * NV * bplane;
         // rotation into the normal basis: swap rows 1 and 2 for y faces
         R ul[NV], ur[NV], f[NV];
@@ -733,7 +814,8 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
         if (kind == 0) {
           const int af = i, b = j;
 #pragma unroll
-          for (int c = 0; c < NV; ++c) fa[c * fa_plane + b * (S.tx + 1) + af] = F[c];
+          for (int c = 0; c < NV; ++c)
+            if (TFV_IN(23, b * (S.tx + 1) + af, fa_plane)) fa[c * fa_plane + b * (S.tx + 1) + af] = F[c];
           if (af == 0 && at_x0) {
 #pragma unroll
             for (int c = 0; c < NV; ++c) bs_a[(0 * S.ty + b) * NV + c] += (double)F[c];
@@ -751,7 +833,8 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
         } else {
           const int a = i, bf = j;
 #pragma unroll
-          for (int c = 0; c < NV; ++c) fb[c * fb_plane + bf * S.tx + a] = F[c];
+          for (int c = 0; c < NV; ++c)
+            if (TFV_IN(24, bf * S.tx + a, fb_plane)) fb[c * fb_plane + bf * S.tx + a] = F[c];
           if (bf == 0 && at_y0) {
 #pragma unroll
             for (int c = 0; c < NV; ++c) bs_b[(0 * S.tx + a) * NV + c] += (double)F[c];
@@ -792,7 +875,9 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
           for (int c = 0; c < NV; ++c) un[c] = Pprev[c] - cu[MD] * (Fm[c] - Fprev[c]);
           const int64_t off = (int64_t)(it - 1) * g.ps + (int64_t)(y0 + ob) * g.na + (x0 + oa);
 #pragma unroll
-          for (int c = 0; c < NV; ++c) Un[c * g.cs + off] = un[c];
+          for (int c = 0; c < NV; ++c)
+            if (TFV_IN(25, off, g.cs) && TFV_OUTSIDE(60, Un + c * g.cs + off, A.ws_lo, A.ws_hi))
+              Un[c * g.cs + off] = un[c];
           if (!physical_cell<R, NV>(un)) bad = true;
           R w[DIM];
           wave_speeds<R, DIM>(un, gprev, w);
@@ -935,7 +1020,9 @@ __global__ void __launch_bounds__(256) fallback_kernel(StepArgs A) {
   constexpr int NV = DIM + 2;
   __shared__ double red[40];
   for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
+    if (!TFV_IN(28, t, A.ntiles)) continue;
     const Tile T = A.tiles[t];
+    if (!TFV_IN(29, T.inst, A.ninst)) continue;
     const InstDesc& d = A.desc[T.inst];
     InstState& st = A.st[T.inst];
     if (st.status != kReady || st.fb_word == 0) continue;  // uniform
@@ -1020,7 +1107,9 @@ __global__ void __launch_bounds__(256) fallback_kernel(StepArgs A) {
         }
         const int64_t off = (int64_t)p * g.ps + (int64_t)b * g.na + a;
 #pragma unroll
-        for (int c = 0; c < NV; ++c) Un[c * g.cs + off] = un[c];
+        for (int c = 0; c < NV; ++c)
+          if (TFV_IN(26, off, g.cs) && TFV_OUTSIDE(61, Un + c * g.cs + off, A.ws_lo, A.ws_hi))
+            Un[c * g.cs + off] = un[c];
         if (!physical_cell<R, NV>(un)) bad = true;
         R w[DIM];
         wave_speeds<R, DIM>(un, gc, w);
@@ -1056,7 +1145,9 @@ __global__ void __launch_bounds__(256) waves_kernel(StepArgs A) {
   constexpr int NV = DIM + 2;
   __shared__ double red[40];
   for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
+    if (!TFV_IN(30, t, A.ntiles)) continue;
     const Tile T = A.tiles[t];
+    if (!TFV_IN(31, T.inst, A.ninst)) continue;
     const InstDesc& d = A.desc[T.inst];
     const InstState& st = A.st[T.inst];
     Geo<DIM> g;
@@ -1078,6 +1169,7 @@ __global__ void __launch_bounds__(256) waves_kernel(StepArgs A) {
     if (owner) {
       for (int p = T.p0; p < T.p1; ++p) {
         const int64_t off = (int64_t)p * g.ps + (int64_t)b * g.na + a;
+        if (!TFV_IN(27, off, g.cs)) continue;
         R u[NV];
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
@@ -1466,6 +1558,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(StepArgs A, int mode, int
   for (int k = 0; k < 15; ++k) s[k] = 0.0;
   for (int k = 0; k < 5; ++k) isum[k] = 0.0;
   for (int t = d.tile0 + threadIdx.x; t < d.tile0 + d.ntiles; t += blockDim.x) {
+    if (!TFV_IN(32, t, A.ntiles)) continue;
     fl |= A.t_flags[t];
     for (int k = 0; k < 3; ++k) w[k] = fmax(w[k], A.t_wmax[(size_t)t * 3 + k]);
     if (mode == 0)

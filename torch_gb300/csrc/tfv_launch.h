@@ -29,6 +29,11 @@ cudaError_t launch_hllc_f64(int nv, int64_t n, const void* ul, const void* ur, c
                             const void* gr, void* out, cudaStream_t s);
 cudaError_t launch_hllc_f32(int nv, int64_t n, const void* ul, const void* ur, const void* gl,
                             const void* gr, void* out, cudaStream_t s);
+#if TFV_CHECKED
+cudaError_t check_read_f64(unsigned long long* out);
+cudaError_t check_read_f32_3d(unsigned long long* out);
+cudaError_t check_read_f32_2d(unsigned long long* out);
+#endif
 cudaError_t launch_finalize(const StepArgs& A, int mode, int fp32, double* integrals_out,
                             cudaStream_t s);
 
