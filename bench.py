@@ -34,6 +34,11 @@ METRIC = "cell-updates/s FP32 vs FP64 plain @L1<1e-5; batched/served p50/p99 lat
 UNIT = "cell-updates/s"
 N = 256
 BYTES_PER_CELL = {"fp32": 40, "fp64": 80}  # read + write of 5 conserved values
+# DRAM bytes of one FP32 step-kernel launch per cell, from one ncu capture of
+# hydro_kernel<float,3,...,16,16> at 192^3 (dram__bytes_read.sum +
+# dram__bytes_write.sum = 153.15 + 104.08 MB for 7,077,888 cells); the traffic
+# grows in proportion to the cells a launch processes.
+TRAFFIC_PER_CELL = (153.15e6 + 104.08e6) / 192 ** 3
 
 
 def explosion_3d(n, nz=None):
@@ -142,6 +147,169 @@ def cpu_reference(steps, warmup, nz=16, workers=1):
     return cells / statistics.median(samples), f"{N}x{N}x{nz} central z-slab, median of {steps} steps"
 
 
+def quadrant(n, rng):
+    """2D quadrant Riemann problem: each quadrant draws rho, p ~ U[0.1, 2] and
+    u, v ~ U[-1, 1]."""
+    c = (np.arange(n) + 0.5) / n
+    Y, X = np.meshgrid(c, c, indexing="ij")
+    q = (X >= 0.5).astype(int) + 2 * (Y >= 0.5).astype(int)
+    vals = np.stack([rng.uniform(0.1, 2, 4), rng.uniform(-1, 1, 4), rng.uniform(-1, 1, 4),
+                     rng.uniform(0.1, 2, 4)])
+    return vals[:, q]
+
+
+def _timed(stream, fn):
+    import torch
+
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    fn()
+    b.record(stream)
+    b.synchronize()
+    return a.elapsed_time(b)
+
+
+def ignition_3d(n):
+    """Nondimensional ignition: rho = 1, T = 1 + 2 exp(-r^2 / (2 * 0.05^2)),
+    p = rho T, at rest, reactant fraction 1."""
+    c = (np.arange(n) + 0.5) / n
+    Z, Y, X = np.meshgrid(c, c, c, indexing="ij")
+    r2 = (X - 0.5) ** 2 + (Y - 0.5) ** 2 + (Z - 0.5) ** 2
+    p = np.zeros((5, n, n, n))
+    p[0] = 1.0
+    p[4] = 1.0 + 2.0 * np.exp(-r2 / (2 * 0.05 ** 2))
+    return p
+
+
+def reactive_leg(n=192, steps=20, warmup=3):
+    """3D reactive ignition, single-step Arrhenius (nondimensional: A = 1e3,
+    Ea/R = 25, q = 20, gamma = 1.2), Van Albada, open boundaries, CFL 0.4:
+    FP32 with FP64 sums against the FP64 plain path after the same steps."""
+    import torch_gb300
+
+    prim = ignition_3d(n)
+    kw = dict(t_end=1e9, cfl=0.4, gamma=1.2, reactive=True, limiter="Albada",
+              max_steps=10 ** 9, chemistry=dict(closure="nondimensional", q_heat=20.0,
+                                                activation_energy=25.0, pre_exponential=1e3))
+    out = {"workload": f"3D reactive ignition {n}^3, nondimensional Arrhenius, Van Albada, "
+                       f"open, CFL 0.4; {steps} timed steps after {warmup}"}
+    sims = {}
+    for prec in ("fp32", "fp64"):
+        sim = torch_gb300.Simulation(prim, [1, 1, 1], precision=prec, graph_steps=1, **kw)
+        sim.advance(warmup)
+        sim.synchronize()
+        ms = _timed(sim._engine.stream, lambda: sim.advance(steps)) / steps
+        sim._engine.refresh()
+        sims[prec] = sim
+        bpc = 48 if prec == "fp32" else 96
+        out[prec] = {"value": n ** 3 / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+                     "steps": sim.steps, "hbm_gbs_at_algorithmic_bytes":
+                         bpc * n ** 3 / (ms * 1e-3) / 1e9, "bytes_per_cell": bpc}
+    r32, r64 = sims["fp32"].device_state[0].double(), sims["fp64"].device_state[0].double()
+    out["fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    out["l1_rho"] = float((r32 - r64).abs().mean())
+    out["linf_rho"] = float((r32 - r64).abs().max())
+    l32 = sims["fp32"]._engine.current_lam().double()
+    l64 = sims["fp64"]._engine.current_lam().double()
+    out["l1_lambda"] = float((l32 - l64).abs().mean())
+    out["fp32_balance_rel"] = float(np.max(np.abs(sims["fp32"].balance_residual))
+                                    / np.max(np.abs(sims["fp32"].initial_integral)))
+    return out
+
+
+def batched_leg(steps=500, count=64, seed=4, fp64_steps=20):
+    """64 quadrant grids (N from {64..1024}), MINBEE, FP32, `steps` steps each
+    in one batch (autotuned tile, graph-captured), against the same grids
+    solved one after another alone (FP32, and the plain FP64 path)."""
+    from torch_gb300 import autotune
+    from torch_gb300.batch import Batch, Grid
+
+    rng = np.random.default_rng(seed)
+    sizes = [int(n) for n in rng.choice([64, 128, 256, 512, 1024], size=count)]
+    prims = [quadrant(n, rng) for n in sizes]
+
+    def grid(p, prec, max_steps=steps):
+        return Grid(p, [1, 1], precision=prec, t_end=1e9, limiter="MINBEE", max_steps=max_steps)
+
+    cells = sum(n * n for n in sizes)
+    t0 = time.perf_counter()
+    tile = autotune.tune([grid(p, "fp32") for p in prims])
+    tune_s = time.perf_counter() - t0
+    grids = [grid(p, "fp32") for p in prims]
+    b = Batch(grids, tile=tile, graph_steps=10)
+    ms = _timed(b.stream, lambda: b.advance(steps))
+    b.refresh()
+    done = sum(g.steps == steps for g in grids)
+    b.close()
+    del b, grids
+    seq32 = 0.0
+    for p in prims:  # each grid alone, same tile and graphs
+        g = grid(p, "fp32")
+        s = Batch([g], tile=tile, graph_steps=10)
+        seq32 += _timed(s.stream, lambda: s.advance(steps))
+        s.close()
+    seq64 = 0.0
+    for p in prims:  # plain FP64 path alone, default tile, timed over fp64_steps
+        g = grid(p, "fp64", fp64_steps + 2)
+        s = Batch([g])
+        s.advance(2)
+        seq64 += _timed(s.stream, lambda: s.advance(fp64_steps)) * steps / fp64_steps
+        s.close()
+    upd = cells * steps
+    return {
+        "workload": f"{count} 2D quadrant Riemann grids, N in {{64..1024}} (seed {seed}), "
+                    f"MINBEE, FP32, {steps} steps each, one batch",
+        "grids": count, "cells": cells, "steps": steps, "grids_completed": done,
+        "tile": list(tile), "autotune_s": tune_s,
+        "value": upd / (ms * 1e-3), "unit": UNIT, "batch_ms": ms,
+        "sequential_fp32": {"value": upd / (seq32 * 1e-3), "ms": seq32},
+        "sequential_fp64_plain": {"value": upd / (seq64 * 1e-3), "ms": seq64,
+                                  "timed_steps_per_grid": fp64_steps},
+        "speedup_vs_sequential_fp32": seq32 / ms,
+        "speedup_vs_sequential_fp64": seq64 / ms,
+        "latency": "every grid finishes with the batch: p50 = p99 = batch_ms",
+    }
+
+
+def served_leg(rates=(10.0, 100.0, 1000.0), count=16, budget_gib=32.0, seed=0):
+    """Poisson request streams of the served mix (40% 1D tubes, 40% 2D, 20% 3D
+    explosions at full size, t_end ~ U[0.1, 0.3]) through the continuous
+    batching server, FP32; against sequential plain FP64 solves of the same
+    requests (each request's FP64 step time alone x its step count)."""
+    from torch_gb300.batch import Batch
+    from torch_gb300.serve import Server, served_requests
+
+    out = []
+    for k, lam in enumerate(rates):
+        reqs = served_requests(rate=lam, count=count, seed=seed + k)
+        srv = Server(budget_bytes=int(budget_gib * (1 << 30)), precision="fp32",
+                     steps_per_tick=8)
+        st = srv.run(reqs)
+        seq_ms = 0.0
+        for r in reqs:  # FP64 alone: 2 warm-up + 3 timed steps, scaled to the request's steps
+            g = r.make_grid("fp64", srv.device)
+            s = Batch([g])
+            s.advance(2)
+            seq_ms += _timed(s.stream, lambda: s.advance(3)) / 3 * max(r.steps, 1)
+            s.close()
+            del s, g
+        upd = st["cell_updates"]
+        out.append({
+            "rate_per_s": lam, "requests": count, "completed": st["completed"],
+            "p50_latency_s": st["p50_latency_s"], "p99_latency_s": st["p99_latency_s"],
+            "wall_s": st["wall_s"], "cell_updates": upd,
+            "value": st["cell_updates_per_s"], "unit": UNIT,
+            "sequential_fp64_plain": {"value": upd / (seq_ms * 1e-3), "s": seq_ms * 1e-3},
+            "speedup_vs_sequential_fp64": (upd / st["wall_s"]) / (upd / (seq_ms * 1e-3)),
+            "mix": {d: sum(r.dim == d for r in reqs) for d in (1, 2, 3)},
+            "rebuilds": srv.rebuilds,
+        })
+    return {"workload": "served mix: 40% 1D tubes N~logU[1e3,1e5], 40% 2D N^2 N~U[128,1024], "
+                        "20% 3D N^3 N~U[64,256]; rho,p~U[0.1,2], t_end~U[0.1,0.3]; VanLeer or "
+                        f"Superbee; FP32, HBM budget {budget_gib} GiB; {count} requests per rate",
+            "sweep": out}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -171,6 +339,10 @@ def main():
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--tile", default=None, help="tx,ty,chunk[,persistent_ctas] of the FP32 step")
+    ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-reactive", action="store_true")
+    ap.add_argument("--skip-served", action="store_true")
+    ap.add_argument("--served-count", type=int, default=16)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -291,6 +463,13 @@ def main():
         }
         del p64
 
+    if rank == 0 and not args.skip_reactive:
+        extra["reactive"] = reactive_leg()
+    if rank == 0 and not args.skip_batched:
+        extra["batched"] = batched_leg()
+    if rank == 0 and not args.skip_served:
+        extra["served"] = served_leg(count=args.served_count)
+
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
         v, sample = cpu_reference(3, 1, workers=1)
@@ -308,7 +487,10 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single",
                        "tile": list(tile) if tile else "default"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+                         "frac": achieved / hbm, "traffic": TRAFFIC_PER_CELL * cells,
+                         "traffic_unit": "DRAM bytes per step-kernel launch (ncu capture of "
+                                         "the 16x16 kernel at 192^3, scaled by cells)",
+                         "peak_kind": peak_kind,
                          "kernel": "hydro_kernel<float,3>", "kernel_ms": step_kernel_ms,
                          "bytes_per_cell": BYTES_PER_CELL["fp32"]},
             "cpu_baseline": cpu,

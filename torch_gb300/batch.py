@@ -172,12 +172,36 @@ class Batch:
                     C.memmove(C.byref(reps[i]), C.byref(r), C.sizeof(_lib.Report))
             _lib.check(self.lib.tfv_batch_restore(handle, reps))
         self.reports = (_lib.Report * len(grids))()
+        self._ev = None
+        self._pending = 0
         self.refresh()
         if graph_steps:
             _lib.check(self.lib.tfv_batch_use_graph(handle, int(graph_steps)))
 
     def advance(self, nsteps):
         _lib.check(self.lib.tfv_batch_advance(self.handle, int(nsteps)))
+
+    def advance_async(self, nsteps):
+        """Enqueue `nsteps` steps bracketed by timing events; `idle()` tells
+        when they are done and `last_ms()` how long they took."""
+        if self._ev is None:
+            self._ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        self._ev[0].record(self.stream)
+        self.advance(nsteps)
+        self._ev[1].record(self.stream)
+        self._pending = int(nsteps)
+
+    def idle(self):
+        return self._pending == 0 or self._ev[1].query()
+
+    def last_ms(self):
+        """(milliseconds, steps) of the last advance_async, once idle."""
+        if self._pending == 0:
+            return None
+        ms = self._ev[0].elapsed_time(self._ev[1])
+        k = self._pending
+        self._pending = 0
+        return ms, k
 
     def refresh(self):
         _lib.check(self.lib.tfv_batch_report(self.handle, self.reports))

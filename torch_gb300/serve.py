@@ -6,7 +6,7 @@ HBM budget, keeps every admitted grid resident until it completes, and
 advances all resident grids of one dimension together with one launch per
 stage (``batch.Batch``), each dimension on its own CUDA stream so that 1D,
 2D and 3D work overlaps.  Grids that finish leave their batch and free their
-memory; waiting requests take their place at the next tick.  Results of a
+memory; waiting requests join when their dimension's batch next goes idle.  Results of a
 grid are the same alone and in the mix: every grid keeps its own dt and the
 per-cell arithmetic does not depend on what else is resident.
 
@@ -99,14 +99,27 @@ def served_requests(rate, count, seed=0, n1=(1e3, 1e5), n2=(128, 1024), n3=(64, 
 
 
 class Server:
-    """Admit, batch and advance requests until all are done."""
+    """Admit, batch and advance requests until all are done.
+
+    One batch per dimension, each on its own CUDA stream.  The host loop polls
+    the batches: a batch whose enqueued steps are done is refreshed, loses its
+    finished grids and gains newly admitted ones (a rebuild), and is given its
+    next slice of steps.  Slices are sized per batch from its measured step
+    time so that each slice takes about `slice_ms` on the device: a batch of
+    small 1D tubes takes hundreds of steps per slice while a batch holding a
+    256^3 grid takes one or two, and neither waits for the other.
+    """
 
     def __init__(self, budget_bytes, precision="fp32", steps_per_tick=8, tile=None,
-                 device=None, max_resident=256, clock=time.perf_counter, keep_results=False):
+                 device=None, max_resident=256, clock=time.perf_counter, keep_results=False,
+                 graphs=True, slice_ms=2.0, max_slice=512):
         self.keep_results = keep_results
+        self.graphs = graphs  # each batch replays a captured graph of `steps_per_tick` steps
         self.budget = int(budget_bytes)
         self.precision = precision
         self.k = int(steps_per_tick)
+        self.slice_ms = float(slice_ms)
+        self.max_slice = int(max_slice)
         self.tiles = tile or {}
         self.device = torch.device(device) if device is not None else torch.device(
             "cuda", torch.cuda.current_device())
@@ -115,6 +128,7 @@ class Server:
         self.used = 0
         self.resident = {1: [], 2: [], 3: []}
         self.batches = {}
+        self.slice = {1: self.k, 2: self.k, 3: self.k}
         self.streams = {d: torch.cuda.Stream(self.device) for d in (1, 2, 3)}
         self.ticks = 0
         self.rebuilds = 0
@@ -125,12 +139,38 @@ class Server:
             old.close()
         grids = [r.grid for r in self.resident[dim]]
         if grids:
-            self.batches[dim] = Batch(grids, tile=self.tiles.get(dim), stream=self.streams[dim])
+            self.batches[dim] = Batch(grids, tile=self.tiles.get(dim), stream=self.streams[dim],
+                                      graph_steps=self.k if self.graphs else 0)
             self.rebuilds += 1
+
+    def _retire(self, dim, t0):
+        """Refresh an idle batch; finished grids leave.  True if any left."""
+        b = self.batches[dim]
+        timing = b.last_ms()
+        if timing is not None and timing[0] > 0:
+            per_step = timing[0] / timing[1]
+            self.slice[dim] = max(1, min(self.max_slice, int(self.slice_ms / per_step)))
+        b.refresh()
+        still, left = [], False
+        for r in self.resident[dim]:
+            if r.grid.done:
+                r.finished = self.clock() - t0
+                r.steps = r.grid.steps
+                r.status = r.grid.status
+                if self.keep_results:
+                    r.result = r.grid.state_host()
+                self.used -= r.bytes_estimate(self.precision)
+                r.grid = None
+                left = True
+            else:
+                still.append(r)
+        self.resident[dim] = still
+        return left
 
     def run(self, requests: List[Request]):
         pending = sorted(requests, key=lambda r: r.arrival)
         waiting = []
+        dirty = set()  # dimensions whose membership changed since their batch was built
         t0 = self.clock()
         i = 0
         while i < len(pending) or waiting or any(self.resident.values()):
@@ -138,7 +178,6 @@ class Server:
             while i < len(pending) and pending[i].arrival <= now:
                 waiting.append(pending[i])
                 i += 1
-            changed = set()
             keep = []
             for r in waiting:  # admission in arrival order while memory allows
                 need = r.bytes_estimate(self.precision)
@@ -149,38 +188,31 @@ class Server:
                     r.admitted = self.clock() - t0
                     self.used += need
                     self.resident[r.dim].append(r)
-                    changed.add(r.dim)
+                    dirty.add(r.dim)
                 else:
                     keep.append(r)
             waiting = keep
-            for d in changed:
-                self._rebuild(d)
-            if not self.batches:
-                if i < len(pending):
-                    time.sleep(max(0.0, min(0.01, pending[i].arrival - (self.clock() - t0))))
-                continue
-            for b in self.batches.values():
-                b.advance(self.k)
-            self.ticks += 1
-            done_dims = set()
-            for d, b in list(self.batches.items()):
-                b.refresh()
-                still = []
-                for r in self.resident[d]:
-                    if r.grid.done:
-                        r.finished = self.clock() - t0
-                        r.steps = r.grid.steps
-                        r.status = r.grid.status
-                        if self.keep_results:
-                            r.result = r.grid.state_host()
-                        self.used -= r.bytes_estimate(self.precision)
-                        r.grid = None
-                        done_dims.add(d)
-                    else:
-                        still.append(r)
-                self.resident[d] = still
-            for d in done_dims:
-                self._rebuild(d)
+            issued = False
+            for d in (1, 2, 3):
+                b = self.batches.get(d)
+                if b is not None:
+                    if not b.idle():
+                        continue
+                    if self._retire(d, t0):
+                        dirty.add(d)
+                if d in dirty:
+                    self._rebuild(d)
+                    dirty.discard(d)
+                b = self.batches.get(d)
+                if b is not None and not b.all_done():
+                    b.advance_async(self.slice[d])
+                    issued = True
+            if issued:
+                self.ticks += 1
+            elif i < len(pending) and not any(self.resident.values()) and not waiting:
+                time.sleep(max(0.0, min(0.01, pending[i].arrival - (self.clock() - t0))))
+            else:
+                time.sleep(5e-5)
         for b in self.batches.values():
             b.close()
         self.batches = {}
