@@ -301,6 +301,37 @@ def large_cfl_case(R):
     np.savez_compressed(OUT / "cfl08_2d.npz", **out)
 
 
+def exact_riemann_cases():
+    """The reference's exact Riemann solver (torchAnalysis.exact_riemann_sod)
+    on Sod and on shock / rarefaction pairs with nonzero velocities.  The
+    module imports matplotlib at top level; a stub module stands in for it."""
+    for name in ("matplotlib", "matplotlib.pyplot"):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    sys.modules["matplotlib"].use = lambda *a, **k: None
+    analysis = importlib.import_module("cfdSolver.torchAnalysis")
+    cases = {
+        "sod": dict(),
+        "sod_t02": dict(t=0.2),
+        "strong": dict(t=0.012, rho_l=1.0, u_l=0.0, p_l=1000.0, rho_r=1.0, u_r=0.0, p_r=0.01),
+        "two_rarefactions": dict(t=0.15, rho_l=1.0, u_l=-2.0, p_l=0.4, rho_r=1.0, u_r=2.0,
+                                 p_r=0.4),
+        "collision": dict(t=0.035, rho_l=5.99924, u_l=19.5975, p_l=460.894, rho_r=5.99242,
+                          u_r=-6.19633, p_r=46.095, x0=0.4),
+    }
+    out = {}
+    x = (np.arange(200) + 0.5) / 200
+    for name, kw in cases.items():
+        kw = dict(kw)
+        kw.setdefault("t", 0.08)
+        rho, u, p = analysis.exact_riemann_sod(x, **kw)
+        out[f"{name}_x"] = x
+        out[f"{name}_rho"], out[f"{name}_u"], out[f"{name}_p"] = rho, u, p
+        out[f"{name}_args"] = np.array([kw.get(k, d) for k, d in (
+            ("t", 0.2), ("x0", 0.5), ("gamma", 1.4), ("rho_l", 1.0), ("u_l", 0.0),
+            ("p_l", 1.0), ("rho_r", 0.125), ("u_r", 0.0), ("p_r", 0.1))])
+    np.savez_compressed(OUT / "exact_riemann.npz", **out)
+
+
 def main():
     R = load_reference()
     rng = np.random.default_rng(20261203)
@@ -310,6 +341,7 @@ def main():
     chemistry_cases(R, rng)
     session_cases(R, rng)
     large_cfl_case(R)
+    exact_riemann_cases()
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -142,3 +142,21 @@ def test_large_cfl_2d_trajectory_matches_reference():
         assert dt == g["dts"][k]
         state = fv.hydro_2d(state, h[0], h[1], dt, 1.4, "VanLeer", "Open", "Open")[0]
     np.testing.assert_array_equal(state, g["state"])
+
+
+def test_exact_riemann_solver_matches_reference():
+    """The oracle's exact Riemann solver (used by the Sod parity tests)
+    against the reference's exact_riemann_sod on Sod, a strong shock, two
+    rarefactions and a shock collision."""
+    from oracle import exact_riemann
+
+    g = np.load(GOLDEN / "exact_riemann.npz")
+    names = sorted({k.rsplit("_", 1)[0] for k in g.files if k.endswith("_args")})
+    assert len(names) == 5
+    for name in names:
+        t, x0, gamma, rl, ul, pl, rr, ur, pr = g[f"{name}_args"]
+        rho, u, p = exact_riemann.sample((rl, ul, pl), (rr, ur, pr), g[f"{name}_x"], t, x0, gamma)
+        for got, key in ((rho, "rho"), (u, "u"), (p, "p")):
+            want = g[f"{name}_{key}"]
+            np.testing.assert_allclose(got, want, rtol=1e-6, atol=1e-7 * np.abs(want).max(),
+                                       err_msg=f"{name} {key}")
