@@ -361,6 +361,8 @@ def main():
     ap.add_argument("--skip-reactive", action="store_true")
     ap.add_argument("--skip-served", action="store_true")
     ap.add_argument("--served-count", type=int, default=16)
+    ap.add_argument("--graph-steps", type=int, default=10,
+                    help="steps captured per CUDA graph in the headline run")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -387,7 +389,8 @@ def main():
     if args.tile:
         vals = [int(v) for v in args.tile.split(",")]
         tile = tuple((vals + [0, 1][len(vals) - 3:])[:5]) if len(vals) < 5 else tuple(vals[:5])
-    sim = torch_gb300.Simulation(prim, [1, 1, 1], precision="fp32", graph_steps=1, tile=tile, **kw)
+    sim = torch_gb300.Simulation(prim, [1, 1, 1], precision="fp32", graph_steps=args.graph_steps,
+                                 tile=tile, **kw)
     eng = sim._engine
     stream = eng.stream
     cells = n ** 3
@@ -504,12 +507,15 @@ def main():
                                          "the 16x16 kernel at 192^3, scaled by cells)",
                          "peak_kind": peak_kind,
                          "kernel": "hydro_kernel<float,3>", "kernel_ms": step_kernel_ms,
+                         "stage_ms": {"step_kernel": step_kernel_ms, "fallback": t_fb / k,
+                                      "finalize": t_fin / k},
                          "bytes_per_cell": BYTES_PER_CELL["fp32"]},
             "cpu_baseline": cpu,
             "e2e": {"value": world * cells / (e2e_ms * 1e-3), "unit": UNIT,
                     "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                     "ms_per_step": e2e_ms},
             "gpu_launches": 3 * args.steps,
+            "graph_steps": args.graph_steps,
             "clocks": clocks.summary(),
             "steps_completed": steps_done,
             "fallback_steps": sim.fallback_steps,

@@ -257,7 +257,8 @@ __global__ void __launch_bounds__(256) waves1d_kernel(StepArgs A) {
     const int ax = min(A.tx, n - T.x0);
     const int i = T.x0 + (int)threadIdx.x;
     const bool owner = (int)threadIdx.x < ax;
-    double ws = 0.0, wh = 0.0, sum[3] = {0.0, 0.0, 0.0};
+    R ws = R(0), wh = R(0);
+    double sum[3] = {0.0, 0.0, 0.0};
     bool bad = false;
     if (owner) {
       for (int f = i; f <= (i == n - 1 ? n : i); ++f) {  // face i (and face n by the last cell)
@@ -270,7 +271,7 @@ __global__ void __launch_bounds__(256) waves1d_kernel(StepArgs A) {
           if (!TFV_IN(41, f, n + 1)) continue;
           if (!TFV_INSIDE(62, S.waves + k * (n + 1) + f, d.scratch, S.flux + 3 * (n + 1))) continue;
           S.waves[k * (n + 1) + f] = s[k];
-          ws = fmax(ws, (double)fabs(s[k]));
+          ws = fmax(ws, fabs(s[k]));
         }
       }
       R u[3];
@@ -278,13 +279,13 @@ __global__ void __launch_bounds__(256) waves1d_kernel(StepArgs A) {
       const R g = gamma1(d, gam, i);
       R rho, v, p;
       prim1(u, g, rho, v, p);
-      wh = (double)(fabs(v) + sound1(rho, p, g));
+      wh = fabs(v) + sound1(rho, p, g);
       for (int c = 0; c < 3; ++c) sum[c] = (double)u[c];
       bad = !physical_cell<R, 3>(u);
     }
     const int fl = block_or(bad ? kFlagNonphysical : 0, reinterpret_cast<int*>(red));
-    const double mws = block_max(ws, red);
-    const double mwh = block_max(wh, red);
+    const double mws = (double)block_max(ws, red);
+    const double mwh = (double)block_max(wh, red);
     double sm[3];
     for (int c = 0; c < 3; ++c) sm[c] = block_sum(sum[c], red);
     if (threadIdx.x == 0) {

@@ -8,4 +8,5 @@
 #define TFV_WITH_1D 1
 #define TFV_LAUNCH1_NAME launch_step1_f32
 #define TFV_CHECK_READ_NAME check_read_f32_2d
+#define TFV_OCC2_NAME occupancy2_f32
 #include "tfv_inst.inc"

@@ -11,4 +11,5 @@
 #define TFV_HLLC_NAME launch_hllc_f32
 #define TFV_WITH_1D 0
 #define TFV_CHECK_READ_NAME check_read_f32_3d
+#define TFV_OCC3_NAME occupancy3_f32
 #include "tfv_inst.inc"

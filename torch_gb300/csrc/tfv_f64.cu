@@ -13,12 +13,15 @@
 #define TFV_WITH_1D 1
 #define TFV_LAUNCH1_NAME launch_step1_f64
 #define TFV_CHECK_READ_NAME check_read_f64
+#define TFV_OCC2_NAME occupancy2_f64
+#define TFV_OCC3_NAME occupancy3_f64
 #include "tfv_inst.inc"
 
 namespace tfv {
 cudaError_t launch_finalize(const StepArgs& A, int mode, int fp32, double* integrals_out,
                             cudaStream_t s) {
-  finalize_kernel<<<A.ninst, 256, 0, s>>>(A, mode, fp32, integrals_out);
+  const dim3 grid(A.fin_slices > 0 ? A.fin_slices : 1, A.ninst);
+  finalize_kernel<<<grid, kFinalizeThreads, 0, s>>>(A, mode, fp32, integrals_out);
   return cudaGetLastError();
 }
 }  // namespace tfv

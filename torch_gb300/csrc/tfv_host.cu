@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstdio>
 #include <cstdint>
@@ -65,7 +66,9 @@ struct tfv_batch {
          off_flags = 0, off_int = 0, off_gam = 0, off_tmaps = 0, total = 0;
   std::vector<CUtensorMap> tmaps;  // [n][4]: ring buffers 0..2, gamma
   size_t gam_bytes = 0;
-  size_t off_mflux = 0, mflux_bytes = 0, off_scratch = 0;
+  size_t off_mflux = 0, mflux_bytes = 0, off_scratch = 0, off_fin = 0, off_cnt = 0;
+  int fin_slices = 1;
+  int sms = 0;  // SMs of the bound device
   unsigned char* ws = nullptr;
   cudaStream_t stream = nullptr;
   StepArgs args{};
@@ -137,6 +140,101 @@ void build_tiles(tfv_batch* b) {
   }
 }
 
+// Resident step-kernel CTAs on the current device (SMs x CTAs per SM), or 0
+// when no device is available or the launch is persistent.
+int resident_slots(const tfv_batch* b) {
+  if (b->dim == 1 || b->tile.persistent_ctas > 0) return 0;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();  // no device here: keep the plain tiling
+    return 0;
+  }
+  const bool f64 = b->precision == TFV_FP64;
+  int per_sm = 0;
+  if (b->dim == 3)
+    per_sm = f64 ? occupancy3_f64(b->varg, b->tile.tx, b->tile.ty)
+                 : occupancy3_f32(b->varg, b->tile.tx, b->tile.ty);
+  else
+    per_sm = f64 ? occupancy2_f64(b->varg, b->tile.tx) : occupancy2_f32(b->varg, b->tile.tx);
+  cudaGetLastError();
+  return per_sm > 0 ? per_sm * sms : 0;
+}
+
+// Completion time of `dur` dispatched in order onto `slots` resident CTAs
+// (each block starts on the first slot that frees up).
+double dispatch_makespan(const std::vector<double>& dur, int slots) {
+  std::vector<double> heap(static_cast<size_t>(slots), 0.0);
+  double end = 0.0;
+  for (double d : dur) {
+    std::pop_heap(heap.begin(), heap.end(), std::greater<double>());
+    heap.back() += d;
+    end = std::max(end, heap.back());
+    std::push_heap(heap.begin(), heap.end(), std::greater<double>());
+  }
+  return end;
+}
+
+// Wave-quantisation fix: when a launch's tiles leave its last wave of
+// resident CTAs partly idle, split the final `slots` tiles along the
+// marching axis into halves, so that the tail is made of short tiles.  The
+// split is kept only where the dispatch model predicts a shorter launch.
+void split_tail(tfv_batch* b) {
+  const int slots = resident_slots(b);
+  if (slots <= 0 || b->dim == 1) return;
+  const int tx = b->tile.tx, ty = b->dim == 3 ? b->tile.ty : 1;
+  auto weight = [&](const Tile& t) {
+    const InstDesc& d = b->desc[t.inst];
+    const int ax = std::min(tx, d.n[0] - t.x0);
+    const int by = b->dim == 3 ? std::min(ty, d.n[1] - t.y0) : 1;
+    const double area = 0.3 + 0.7 * double(ax * by) / double(tx * ty);
+    return area * (double(t.p1 - t.p0) + 2.0);  // + the chunk's extra plane and fixed cost
+  };
+  std::vector<Tile> out;
+  out.reserve(b->tiles.size() + slots);
+  for (const auto& g : b->groups) {
+    std::vector<double> plain, split;
+    const int first_split = std::max(g.t_begin, g.t_end - slots);
+    for (int t = g.t_begin; t < g.t_end; ++t) {
+      const Tile& T = b->tiles[t];
+      plain.push_back(weight(T));
+      if (t >= first_split && T.p1 - T.p0 >= 8) {
+        Tile a = T, c = T;
+        a.p1 = c.p0 = T.p0 + (T.p1 - T.p0) / 2;
+        split.push_back(weight(a));
+        split.push_back(weight(c));
+      } else {
+        split.push_back(weight(T));
+      }
+    }
+    const bool use = dispatch_makespan(split, slots) < 0.99 * dispatch_makespan(plain, slots);
+    for (int t = g.t_begin; t < g.t_end; ++t) {
+      const Tile& T = b->tiles[t];
+      if (use && t >= first_split && T.p1 - T.p0 >= 8) {
+        Tile a = T, c = T;
+        a.p1 = c.p0 = T.p0 + (T.p1 - T.p0) / 2;
+        out.push_back(a);
+        out.push_back(c);
+      } else {
+        out.push_back(T);
+      }
+    }
+  }
+  if (out.size() == b->tiles.size()) return;
+  b->tiles.swap(out);
+  // tiles of an instance stay contiguous: recompute ranges and groups
+  for (int i = 0; i < b->n; ++i) b->desc[i].ntiles = 0;
+  b->groups.clear();
+  for (int t = 0; t < (int)b->tiles.size(); ++t) {
+    InstDesc& d = b->desc[b->tiles[t].inst];
+    if (d.ntiles == 0) d.tile0 = t;
+    ++d.ntiles;
+    const int lim = b->cfg[b->tiles[t].inst].limiter;
+    if (b->groups.empty() || b->groups.back().limiter != lim) b->groups.push_back({lim, t, t});
+    b->groups.back().t_end = t + 1;
+  }
+}
+
 void fill_desc(tfv_batch* b, int i) {
   const tfv_config& c = b->cfg[i];
   InstDesc& d = b->desc[i];
@@ -201,6 +299,13 @@ void layout(tfv_batch* b) {
   o = align_up(o + sizeof(int32_t) * nt, 256);
   b->off_int = o;
   o = align_up(o + sizeof(double) * 5 * b->n, 256);
+  b->fin_slices = 1;
+  for (int i = 0; i < b->n; ++i)
+    b->fin_slices = std::max(b->fin_slices, (b->desc[i].ntiles + 255) / 256);
+  b->off_fin = o;  // finalize slice records [n][fin_slices][24] and counters [n]
+  o = align_up(o + sizeof(double) * 24 * b->fin_slices * b->n, 256);
+  b->off_cnt = o;
+  o = align_up(o + sizeof(int32_t) * b->n, 256);
   b->off_tmaps = o;
   o = align_up(o + sizeof(CUtensorMap) * 4 * b->n, 256);
   b->off_gam = o;
@@ -389,7 +494,10 @@ cudaError_t launch_range_unchecked(tfv_batch* b, int op, int lim, int t0, int t1
   A.dst_off = dst_off;
   A.t_begin = t0;
   A.t_end = t1;
-  const int grid = grid_for(b, t1 - t0);
+  // the fallback usually exits at once (no tile flagged): two CTAs per SM
+  // walk the tiles instead of one CTA per tile
+  const int grid = op == kOpFallback ? std::min(grid_for(b, t1 - t0), std::max(2 * b->sms, 1))
+                                     : grid_for(b, t1 - t0);
   if (b->precision == TFV_FP64) {
     if (b->dim == 1) return launch_step1_f64(op, b->varg, lim, A, grid, b->block, b->stream);
     return b->dim == 3 ? launch_step3_f64(op, b->varg, lim, A, grid, b->block, b->stream)
@@ -563,6 +671,7 @@ static int create_internal(int32_t dim, int32_t precision, int32_t n, const tfv_
   b->desc.resize(n);
   for (int i = 0; i < n; ++i) fill_desc(b, i);
   build_tiles(b);
+  split_tail(b);
   layout(b);
   b->st.assign(n, InstState{});
   *out = b;
@@ -614,6 +723,11 @@ int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* con
   }
   b->ws = static_cast<unsigned char*>(workspace);
   b->stream = static_cast<cudaStream_t>(stream);
+  {
+    int dev = 0;
+    TFV_CUDA(cudaGetDevice(&dev));
+    TFV_CUDA(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev));
+  }
   for (int i = 0; i < b->n; ++i) {
     InstDesc& d = b->desc[i];
     for (int k = 0; k < b->nring; ++k) {
@@ -683,6 +797,9 @@ int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* con
   A.t_sum = reinterpret_cast<double*>(b->ws + b->off_sum);
   A.t_flags = reinterpret_cast<int32_t*>(b->ws + b->off_flags);
   A.tmaps = b->ws + b->off_tmaps;
+  A.fin_part = reinterpret_cast<double*>(b->ws + b->off_fin);
+  A.fin_cnt = reinterpret_cast<int32_t*>(b->ws + b->off_cnt);
+  A.fin_slices = b->fin_slices;
   A.ws_lo = b->ws;
   A.ws_hi = b->ws + b->total;
   b->block = b->tile.tx * b->tile.ty;
@@ -693,6 +810,7 @@ int tfv_batch_bind(tfv_batch* b, void* workspace, void* const* states, void* con
                            cudaMemcpyHostToDevice, b->stream));
   TFV_CUDA(cudaMemcpyAsync(b->ws + b->off_tiles, b->tiles.data(), sizeof(Tile) * b->tiles.size(),
                            cudaMemcpyHostToDevice, b->stream));
+  TFV_CUDA(cudaMemsetAsync(b->ws + b->off_cnt, 0, sizeof(int32_t) * b->n, b->stream));
   TFV_CUDA(cudaMemcpyAsync(b->ws + b->off_tmaps, b->tmaps.data(),
                            sizeof(CUtensorMap) * b->tmaps.size(), cudaMemcpyHostToDevice,
                            b->stream));

@@ -32,6 +32,18 @@
 namespace tfv {
 
 enum : int { kBcOpen = 0, kBcReflective = 1, kBcPeriodic = 2, kBcInflow = 3 };
+constexpr int kFinalizeThreads = 256;  // threads of a finalize CTA
+constexpr int kFinalizeSlice = 256;    // tiles reduced by one finalize CTA
+constexpr int kPartVals = 23;          // partials per tile: 3 maxima, 15 boundary sums, 5 integrals
+
+// an int carried in a double slot of the finalize records (bit copy)
+__device__ __forceinline__ double __int_as_double_bits(int v) {
+  return __longlong_as_double((long long)(unsigned)v);
+}
+__device__ __forceinline__ int __double_bits_as_int(double v) {
+  return (int)(unsigned)__double_as_longlong(v);
+}
+
 enum : int { kReady = 0, kDone = 1, kErrMaxSteps = 2, kErrStall = 3, kErrNonphysical = 4,
              kErrReactive = 5, kErrSpecies = 6, kErrChemistry = 7, kRetry = 8,
              kErrDeviceWait = 9 };
@@ -105,6 +117,11 @@ __device__ __forceinline__ double warp_max(double v) {
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
   return v;
 }
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
 __device__ __forceinline__ int warp_or(int v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v |= __shfl_down_sync(0xffffffffu, v, o);
@@ -135,6 +152,22 @@ __device__ __forceinline__ double block_max(double v, double* scratch) {
   double t = 0.0;
   if (threadIdx.x == 0) {
     for (int w = 0; w < nw; ++w) t = fmax(t, scratch[w]);
+  }
+  return t;
+}
+// Single-precision maximum (exact: the result equals the double maximum of
+// the same values) without double-precision arithmetic.
+__device__ __forceinline__ float block_max(float v, double* scratch_d) {
+  float* scratch = reinterpret_cast<float*>(scratch_d);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) scratch[warp] = v;
+  __syncthreads();
+  float t = 0.0f;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < nw; ++w) t = fmaxf(t, scratch[w]);
   }
   return t;
 }
@@ -918,7 +951,7 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   fl = block_or(fl, reinterpret_cast<int*>(red));
   double wm[DIM];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) wm[k] = block_max(owner ? (double)wmax[k] : 0.0, red);
+  for (int k = 0; k < DIM; ++k) wm[k] = (double)block_max(owner ? wmax[k] : R(0), red);
   __syncthreads();
   if (tid == 0) {
     double* out = A.t_bsum + (size_t)t * 15;
@@ -946,8 +979,9 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
 template <typename R, int DIM, bool VARG, int LIM, int TX, int TY>
 __global__ void __launch_bounds__(256, TFV_HYDRO_MIN_BLOCKS) hydro_kernel(StepArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  unsigned char* smem = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  // align by pointer arithmetic on the shared array (an integer round trip
+  // would hide the address space and turn every shared access generic)
+  unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
   HydroSmem<R, DIM, VARG> S;
   S.init(TX > 0 ? TX : A.tx, TY > 0 ? TY : A.ty);
   if (threadIdx.x == 0) {
@@ -1125,7 +1159,7 @@ __global__ void __launch_bounds__(256) fallback_kernel(StepArgs A) {
       for (int c = 0; c < NV; ++c) sums[k][c] = block_sum(acc[k][c], red);
     double wm[DIM];
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) wm[k] = block_max(owner ? (double)wmax[k] : 0.0, red);
+    for (int k = 0; k < DIM; ++k) wm[k] = (double)block_max(owner ? wmax[k] : R(0), red);
     if (threadIdx.x == 0) {
       double* out = A.t_bsum + (size_t)t * 15;
       for (int k = 0; k < DIM; ++k)
@@ -1187,7 +1221,7 @@ __global__ void __launch_bounds__(256) waves_kernel(StepArgs A) {
     int fl = block_or(bad ? kFlagNonphysical : 0, reinterpret_cast<int*>(red));
     double wm[DIM], sm[NV];
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) wm[k] = block_max(owner ? (double)wmax[k] : 0.0, red);
+    for (int k = 0; k < DIM; ++k) wm[k] = (double)block_max(owner ? wmax[k] : R(0), red);
 #pragma unroll
     for (int c = 0; c < NV; ++c) sm[c] = block_sum(sum[c], red);
     if (threadIdx.x == 0) {
@@ -1423,7 +1457,7 @@ __global__ void __launch_bounds__(256) react_kernel(StepArgs A, int stage) {
     fl = block_or(fl, reinterpret_cast<int*>(red));
     double wm[DIM], sm[NV];
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) wm[k] = block_max(owner ? (double)wmax[k] : 0.0, red);
+    for (int k = 0; k < DIM; ++k) wm[k] = (double)block_max(owner ? wmax[k] : R(0), red);
 #pragma unroll
     for (int c = 0; c < NV; ++c) sm[c] = stage == 2 ? block_sum(src[c], red) : 0.0;
     if (threadIdx.x == 0) {
@@ -1540,50 +1574,90 @@ __global__ void gamma_kernel(StepArgs A) {
 }
 
 #ifdef TFV_DEFINE_SHARED_KERNELS  // defined by exactly one translation unit
-__global__ void __launch_bounds__(256) finalize_kernel(StepArgs A, int mode, int fp32,
-                                                       double* integrals_out) {
-  __shared__ double red[40];
-  __shared__ double sh_w[3], sh_s[15], sh_i[5];
-  __shared__ int sh_f;
-  const int i = blockIdx.x;
+__global__ void __launch_bounds__(kFinalizeThreads) finalize_kernel(StepArgs A, int mode,
+                                                                    int fp32,
+                                                                    double* integrals_out) {
+  // Grid (slices, instances).  A slice CTA reduces up to kFinalizeSlice tiles:
+  // value k of the 23 partials (3 wave maxima, 15 boundary sums, 5 integrals)
+  // is summed by kGroups threads over interleaved tiles, then in a fixed
+  // order.  An instance with several slices publishes each slice's record;
+  // the last slice to arrive combines the records in slice order (so the
+  // result does not depend on which slice finished last) and commits.
+  constexpr int NV = kPartVals;
+  constexpr int kGroups = kFinalizeThreads / NV;
+  __shared__ double acc[kFinalizeThreads];
+  __shared__ double sh_v[NV];
+  __shared__ int fred[kFinalizeThreads / 32];
+  __shared__ int sh_f, sh_last;
+  const int i = blockIdx.y;
   if (i >= A.ninst) return;
   const InstDesc& d = A.desc[i];
   InstState& st = A.st[i];
-  if (mode == 0 && st.status != kReady) return;  // uniform
+  if (mode == 0 && st.status != kReady) return;  // uniform over the instance's slices
   if (mode == 4 && st.status != kReady && st.status != kRetry) return;
+  const int nslices = (d.ntiles + kFinalizeSlice - 1) / kFinalizeSlice;
+  const int slice = blockIdx.x;
+  if (slice >= nslices) return;
   const int nv = d.dim + 2;
+  const bool want_s = mode == 0;
+  const bool want_i = mode == 2 || mode == 3 || (mode == 0 && d.reactive);
+  const int t0 = d.tile0 + slice * kFinalizeSlice;
+  const int t1 = min(d.tile0 + d.ntiles, t0 + kFinalizeSlice);
+  const int j = threadIdx.x;
   int fl = 0;
-  double w[3] = {0.0, 0.0, 0.0};
-  double s[15], isum[5];
-  for (int k = 0; k < 15; ++k) s[k] = 0.0;
-  for (int k = 0; k < 5; ++k) isum[k] = 0.0;
-  for (int t = d.tile0 + threadIdx.x; t < d.tile0 + d.ntiles; t += blockDim.x) {
-    if (!TFV_IN(32, t, A.ntiles)) continue;
-    fl |= A.t_flags[t];
-    for (int k = 0; k < 3; ++k) w[k] = fmax(w[k], A.t_wmax[(size_t)t * 3 + k]);
-    if (mode == 0)
-      for (int k = 0; k < 15; ++k) s[k] += A.t_bsum[(size_t)t * 15 + k];
-    if (mode == 2 || mode == 3 || (mode == 0 && d.reactive))
-      for (int k = 0; k < 5; ++k) isum[k] += A.t_sum[(size_t)t * 5 + k];
-  }
-  fl = block_or(fl, reinterpret_cast<int*>(red));
-  if (threadIdx.x == 0) sh_f = fl;
-  for (int k = 0; k < 3; ++k) {
-    const double v = block_max(w[k], red);
-    if (threadIdx.x == 0) sh_w[k] = v;
-  }
-  if (mode == 0) {
-    for (int k = 0; k < 15; ++k) {
-      const double v = block_sum(s[k], red);
-      if (threadIdx.x == 0) sh_s[k] = v;
+  for (int t = t0 + j; t < t1; t += blockDim.x)
+    if (TFV_IN(32, t, A.ntiles)) fl |= A.t_flags[t];
+  fl = block_or(fl, fred);
+  double v = 0.0;
+  if (j < kGroups * NV) {
+    const int k = j % NV, g = j / NV;
+    if (k < 3 || (k < 18 ? want_s : want_i)) {
+      for (int t = t0 + g; t < t1; t += kGroups) {
+        if (!TFV_IN(33, t, A.ntiles)) continue;
+        if (k < 3) v = fmax(v, A.t_wmax[(size_t)t * 3 + k]);
+        else if (k < 18) v += A.t_bsum[(size_t)t * 15 + (k - 3)];
+        else v += A.t_sum[(size_t)t * 5 + (k - 18)];
+      }
     }
   }
-  if (mode == 2 || mode == 3 || (mode == 0 && d.reactive)) {
-    for (int k = 0; k < 5; ++k) {
-      const double v = block_sum(isum[k], red);
-      if (threadIdx.x == 0) sh_i[k] = v;
-    }
+  acc[j] = v;
+  __syncthreads();
+  if (j < NV) {
+    double r = acc[j];
+    for (int g = 1; g < kGroups; ++g) r = j < 3 ? fmax(r, acc[g * NV + j]) : r + acc[g * NV + j];
+    sh_v[j] = r;
   }
+  if (j == 0) sh_f = fl;
+  __syncthreads();
+  if (nslices > 1) {
+    double* part = A.fin_part + ((size_t)i * A.fin_slices + slice) * (NV + 1);
+    if (j < NV) part[j] = sh_v[j];
+    if (j == 0) part[NV] = __int_as_double_bits(sh_f);
+    __threadfence();
+    __syncthreads();
+    if (j == 0) sh_last = atomicAdd(&A.fin_cnt[i], 1) == nslices - 1;
+    __syncthreads();
+    if (!sh_last) return;
+    __threadfence();
+    const double* base = A.fin_part + (size_t)i * A.fin_slices * (NV + 1);
+    if (j < NV) {
+      double r = __ldcg(base + j);
+      for (int q = 1; q < nslices; ++q) {
+        const double x = __ldcg(base + (size_t)q * (NV + 1) + j);
+        r = j < 3 ? fmax(r, x) : r + x;
+      }
+      sh_v[j] = r;
+    } else if (j == 32) {
+      int f = 0;
+      for (int q = 0; q < nslices; ++q) f |= __double_bits_as_int(__ldcg(base + (size_t)q * (NV + 1) + NV));
+      sh_f = f;
+      A.fin_cnt[i] = 0;  // ready for the next launch
+    }
+    __syncthreads();
+  }
+  const double* sh_w = sh_v;
+  const double* sh_s = sh_v + 3;
+  const double* sh_i = sh_v + 18;
   if (threadIdx.x != 0) return;
   if (mode == 2) {
     for (int c = 0; c < 5; ++c) integrals_out[i * 5 + c] = c < nv ? sh_i[c] * d.vol : 0.0;

@@ -34,6 +34,11 @@ cudaError_t check_read_f64(unsigned long long* out);
 cudaError_t check_read_f32_3d(unsigned long long* out);
 cudaError_t check_read_f32_2d(unsigned long long* out);
 #endif
+// Resident step-kernel CTAs per SM for a tile shape (0 when unknown).
+int occupancy2_f64(bool varg, int tx);
+int occupancy3_f64(bool varg, int tx, int ty);
+int occupancy2_f32(bool varg, int tx);
+int occupancy3_f32(bool varg, int tx, int ty);
 cudaError_t launch_finalize(const StepArgs& A, int mode, int fp32, double* integrals_out,
                             cudaStream_t s);
 

@@ -158,7 +158,9 @@ __device__ __forceinline__ bool physical_cell(const R* u) {
     R all = u[0];
 #pragma unroll
     for (int c = 1; c < NV; ++c) all = all + u[c];
-    return finite_(all) && (u[0] > R(kFloor)) && (u[NV - 1] - R(0.5) * s * rcp(u[0]) > R(kFloor));
+    // E - |m|^2 / (2 rho) > floor, multiplied through by rho > floor
+    return finite_(all) && (u[0] > R(kFloor)) &&
+           (u[NV - 1] * u[0] - R(0.5) * s > R(kFloor) * u[0]);
   }
 }
 

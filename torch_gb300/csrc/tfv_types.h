@@ -82,6 +82,9 @@ struct StepArgs {
   double* t_wmax;  // [ntiles][3] max(|u_d| + a) of the new state
   double* t_sum;   // [ntiles][5] integrals / source partial sums
   int32_t* t_flags;// [ntiles] bit0: nonphysical result, bit1: gate, bit2: species
+  double* fin_part;  // [ninst][fin_slices][24] finalize slice records
+  int32_t* fin_cnt;  // [ninst] finalize slices arrived (reset by the last)
+  int32_t fin_slices;
   const unsigned char* ws_lo;  // workspace range (address checks of the checked build)
   const unsigned char* ws_hi;
 };
