@@ -404,6 +404,12 @@ __device__ __forceinline__ void face_flux1(const InstDesc& d, const R* U, const 
 template <typename R, bool VARG>
 __global__ void __launch_bounds__(256) update1d_kernel(StepArgs A, int first_order) {
   __shared__ double red[40];
+  if (first_order) {  // the fallback pass: usually no instance is flagged
+    int any = 0;
+    for (int k = threadIdx.x; k < A.ninst; k += blockDim.x)
+      any |= (A.st[k].status == kReady && A.st[k].fb_word != 0);
+    if (!__syncthreads_or(any)) return;
+  }
   for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
     if (!TFV_IN(45, t, A.ntiles)) continue;
     const Tile T = A.tiles[t];

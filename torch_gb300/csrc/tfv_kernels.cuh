@@ -584,6 +584,22 @@ __device__ __forceinline__ void wave_speeds(const R* u, R g, R* w) {
   }
 }
 
+// FP64 sum over the CTA of the marching-axis boundary fluxes (first and last
+// plane of the domain only).  Kept out of line so that the conversions to
+// double stay on this rare path instead of being hoisted into every plane.
+template <typename R, int NV>
+struct FaceFlux {
+  R v[NV];
+};
+template <typename R, int NV>
+__device__ __noinline__ void march_boundary_sum(FaceFlux<R, NV> ff, double* red, double* out) {
+#pragma unroll
+  for (int c = 0; c < NV; ++c) {
+    const double s = block_sum((double)ff.v[c], red);
+    if (threadIdx.x == 0) out[c] += s;
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ T* smem_at(unsigned char* base, size_t off) {
   return reinterpret_cast<T*>(base + off);
@@ -849,14 +865,6 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
 #pragma unroll
           for (int c = 0; c < NV; ++c)
             if (TFV_IN(23, b * (S.tx + 1) + af, fa_plane)) fa[c * fa_plane + b * (S.tx + 1) + af] = F[c];
-          if (af == 0 && at_x0) {
-#pragma unroll
-            for (int c = 0; c < NV; ++c) bs_a[(0 * S.ty + b) * NV + c] += (double)F[c];
-          }
-          if (af == ax && at_x1) {
-#pragma unroll
-            for (int c = 0; c < NV; ++c) bs_a[(1 * S.ty + b) * NV + c] += (double)F[c];
-          }
           if (want_flux && fout[0]) {
             const int64_t nf = (int64_t)g.na + 1;
 #pragma unroll
@@ -868,14 +876,6 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
 #pragma unroll
           for (int c = 0; c < NV; ++c)
             if (TFV_IN(24, bf * S.tx + a, fb_plane)) fb[c * fb_plane + bf * S.tx + a] = F[c];
-          if (bf == 0 && at_y0) {
-#pragma unroll
-            for (int c = 0; c < NV; ++c) bs_b[(0 * S.tx + a) * NV + c] += (double)F[c];
-          }
-          if (bf == by && at_y1) {
-#pragma unroll
-            for (int c = 0; c < NV; ++c) bs_b[(1 * S.tx + a) * NV + c] += (double)F[c];
-          }
           if (want_flux && fout[1]) {
 #pragma unroll
             for (int c = 0; c < NV; ++c)
@@ -888,6 +888,25 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
     if (__syncthreads_or(!waited_ok)) {  // in-plane fluxes complete; plane it+2 staged
       if (tid == 0) st.status = kErrDeviceWait;
       return false;
+    }
+    if (full && (at_x0 || at_x1 || at_y0 || at_y1)) {
+      // FP64 sums of the domain-boundary in-plane faces, read back from shared
+      // memory by tiles that touch an edge (interior tiles carry no FP64 work);
+      // each entry belongs to one thread and accumulates plane by plane
+      const int nxb = 2 * S.ty * NV;
+      const int nyb = DIM == 3 ? 2 * S.tx * NV : 0;
+      for (int e = tid; e < nxb + nyb; e += NT) {
+        if (e < nxb) {
+          const int side = e / (S.ty * NV), b = (e / NV) % S.ty, c = e % NV;
+          if (b < by && (side ? at_x1 : at_x0))
+            bs_a[e] += (double)fa[c * fa_plane + b * (S.tx + 1) + (side ? ax : 0)];
+        } else {
+          const int q = e - nxb;
+          const int side = q / (S.tx * NV), a = (q / NV) % S.tx, c = q % NV;
+          if (a < ax && (side ? at_y1 : at_y0))
+            bs_b[q] += (double)fb[c * fb_plane + (side ? by : 0) * S.tx + a];
+        }
+      }
     }
     R Fm[NV];
 #pragma unroll
@@ -937,12 +956,10 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
       gprev = gcur;
     }
     if (it >= p0 && (it == 0 || it == g.np)) {  // march-axis boundary faces
-      const int side = it == 0 ? 0 : 1;
+      FaceFlux<R, NV> ff;
 #pragma unroll
-      for (int c = 0; c < NV; ++c) {
-        const double s = block_sum(owner ? (double)Fm[c] : 0.0, red);
-        if (tid == 0) bs_m[side * NV + c] += s;
-      }
+      for (int c = 0; c < NV; ++c) ff.v[c] = owner ? Fm[c] : R(0);
+      march_boundary_sum<R, NV>(ff, red, bs_m + (it == 0 ? 0 : NV));
     }
   }
 
@@ -1053,6 +1070,14 @@ template <typename R, int DIM, bool VARG>
 __global__ void __launch_bounds__(256) fallback_kernel(StepArgs A) {
   constexpr int NV = DIM + 2;
   __shared__ double red[40];
+  {
+    // usually no instance is flagged: one look at the instance states instead
+    // of walking the tile table
+    int any = 0;
+    for (int k = threadIdx.x; k < A.ninst; k += blockDim.x)
+      any |= (A.st[k].status == kReady && A.st[k].fb_word != 0);
+    if (!__syncthreads_or(any)) return;
+  }
   for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
     if (!TFV_IN(28, t, A.ntiles)) continue;
     const Tile T = A.tiles[t];
@@ -1296,6 +1321,45 @@ __device__ __forceinline__ void plan_next(const InstDesc& d, InstState& st, cons
     return;
   }
   st.status = kReady;
+}
+
+// plan_next run by one warp: the independent FP64 divisions (w_d / h_d of the
+// CFL reduction, the dt / h_d coefficients) go to separate lanes.  Every
+// value keeps the expression and operation order of the serial form, so the
+// results are identical; GB300's double-precision pipe is narrow, and a
+// single thread's chain of divisions was the finalize kernel's critical path.
+__device__ __forceinline__ void plan_next_warp(const InstDesc& d, InstState& st, const double* w,
+                                               int fp32, int lane) {
+  if (st.time == d.t_end) {
+    if (lane == 0) st.status = kDone;
+    return;
+  }
+  if (st.steps >= d.max_steps) {
+    if (lane == 0) st.status = kErrMaxSteps;
+    return;
+  }
+  double dt;
+  if (d.dim == 3) {
+    const double q = lane < 3 ? w[lane] / d.h[lane] : 0.0;
+    const double q0 = __shfl_sync(0xffffffffu, q, 0);
+    const double q1 = __shfl_sync(0xffffffffu, q, 1);
+    const double q2 = __shfl_sync(0xffffffffu, q, 2);
+    const double total = (q0 + q1) + q2;
+    dt = d.cfl / total;
+  } else {
+    dt = cfl_dt(d, w);
+  }
+  if (fp32) dt = (double)(float)dt;
+  const double rem = d.t_end - st.time;
+  if (rem < dt) dt = rem;
+  if (lane < 3) {
+    st.coef_half[lane] = (0.5 * dt) / d.h[lane];
+  } else if (lane < 6) {
+    st.coef_full[lane - 3] = dt / d.h[lane - 3];
+  } else if (lane == 6) {
+    st.dt = dt;
+    st.status = (!isfinite(dt) || dt <= 0.0 || st.time + dt == st.time) ? kErrStall : kReady;
+  }
 }
 
 // --------------------------------------------------------------------------
@@ -1658,13 +1722,55 @@ __global__ void __launch_bounds__(kFinalizeThreads) finalize_kernel(StepArgs A, 
   const double* sh_w = sh_v;
   const double* sh_s = sh_v + 3;
   const double* sh_i = sh_v + 18;
-  if (threadIdx.x != 0) return;
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  if (mode == 0) {
+    // commit, one lane per conserved component
+    const int f = sh_f;
+    if (f & (kFlagNonphysical | kFlagSpecies | kFlagChemistry)) {
+      if (lane == 0) {
+        st.status = (f & kFlagNonphysical) ? kErrNonphysical
+                    : (f & kFlagSpecies)   ? kErrSpecies
+                                           : kErrChemistry;
+        st.fb_word = 0;
+      }
+      return;
+    }
+    const double dt = st.dt;
+    if (lane < nv) {
+      double out = 0.0;
+      for (int k = 0; k < d.dim; ++k) out += dt * d.vol / d.h[k] * sh_s[k * 5 + lane];
+      st.boundary[lane] += out;
+      if (d.reactive) st.source[lane] += d.vol * sh_i[lane];
+    }
+    const int fb = st.fb_word;
+    __syncwarp();
+    if (lane == 0) {
+      st.cur = (st.cur + A.dst_off) % d.nring;
+      const double tn = st.time + dt;
+      st.time = tn < d.t_end ? tn : d.t_end;
+      st.steps += 1;
+      st.last_fallback = fb != 0;
+      st.fallback_steps += fb != 0;
+      st.fb_word = 0;
+      st.retry = 0;
+    }
+    __syncwarp();
+    plan_next_warp(d, st, sh_w, fp32, lane);
+    return;
+  }
+  if (mode == 1 || mode == 3) {
+    if (mode == 3 && lane < 5) st.initial[lane] = lane < nv ? sh_i[lane] * d.vol : 0.0;
+    const int status = st.status;
+    if (status != kReady && status != kDone) return;  // plan-only keeps a pending error
+    __syncwarp();
+    plan_next_warp(d, st, sh_w, fp32, lane);
+    return;
+  }
+  if (lane != 0) return;
   if (mode == 2) {
     for (int c = 0; c < 5; ++c) integrals_out[i * 5 + c] = c < nv ? sh_i[c] * d.vol : 0.0;
     return;
-  }
-  if (mode == 3) {
-    for (int c = 0; c < 5; ++c) st.initial[c] = c < nv ? sh_i[c] * d.vol : 0.0;
   }
   if (mode == 4) {
     if (sh_f & kFlagChemistry) {
@@ -1688,41 +1794,6 @@ __global__ void __launch_bounds__(kFinalizeThreads) finalize_kernel(StepArgs A, 
     st.status = kRetry;
     return;
   }
-  if (mode == 0) {
-    if (sh_f & kFlagNonphysical) {
-      st.status = kErrNonphysical;
-      st.fb_word = 0;
-      return;
-    }
-    if (sh_f & kFlagSpecies) {
-      st.status = kErrSpecies;
-      st.fb_word = 0;
-      return;
-    }
-    if (sh_f & kFlagChemistry) {
-      st.status = kErrChemistry;
-      st.fb_word = 0;
-      return;
-    }
-    const double dt = st.dt;
-    for (int c = 0; c < nv; ++c) {
-      double out = 0.0;
-      for (int k = 0; k < d.dim; ++k) out += dt * d.vol / d.h[k] * sh_s[k * 5 + c];
-      st.boundary[c] += out;
-      if (d.reactive) st.source[c] += d.vol * sh_i[c];
-    }
-    st.cur = (st.cur + A.dst_off) % d.nring;
-    const double tn = st.time + dt;
-    st.time = tn < d.t_end ? tn : d.t_end;
-    st.steps += 1;
-    st.last_fallback = st.fb_word != 0;
-    st.fallback_steps += st.fb_word != 0;
-    st.fb_word = 0;
-    st.retry = 0;
-  } else if (st.status != kReady && st.status != kDone) {
-    return;  // plan-only keeps a pending error
-  }
-  plan_next(d, st, sh_w, fp32);
 }
 
 #endif  // TFV_DEFINE_SHARED_KERNELS
