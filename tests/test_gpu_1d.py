@@ -58,6 +58,9 @@ def test_1d_reactive_znd_matches_reference():
     np.testing.assert_allclose(gpu.state, g[f"{name}_state"], rtol=1e-10)
     np.testing.assert_allclose(gpu.lam, g[f"{name}_lam"], rtol=1e-10, atol=1e-14)
     np.testing.assert_allclose(gpu.beta, g[f"{name}_beta"], rtol=1e-10, atol=1e-14)
+    np.testing.assert_allclose(gpu.source_integral, g[f"{name}_source"], rtol=1e-8, atol=1e-6)
+    np.testing.assert_allclose(gpu.boundary_integral, g[f"{name}_boundary"], rtol=1e-8,
+                               atol=1e-10)
 
 
 def sod(n, left=(1.0, 0.0, 1.0), right=(0.125, 0.0, 0.1)):
@@ -130,3 +133,26 @@ def test_1d_many_tiles_fp64_bitwise_and_fp32_close():
     assert s32.steps == s64.steps == 210
     assert np.mean(np.abs(s32.state[0] - s64.state[0])) <= 1e-5
     assert np.max(np.abs(s32.balance_residual) / np.abs(s32.initial_integral).max()) < 1e-6
+
+
+def test_1d_arrhenius_source_integral_matches_oracle():
+    """Heat release in a 1D tube (SI Arrhenius, fast kinetics): the source
+    integral, state and reactant fraction follow the oracle.  The second
+    reaction half step's source sums must reach the commit unchanged."""
+    n = 200
+    x = (np.arange(n) + 0.5) / n
+    p = np.zeros((3, n))
+    p[0] = 1.0
+    p[2] = np.where(x < 0.3, 4e6, 101325.0)
+    kw = dict(t_end=1e-3, reactive=True, kinetic_model="arrhenius",
+              chemistry=dict(pre_exponential=1e9), limiter="VanLeer")
+    ref = OracleSimulation(p, [1.0], **kw)
+    gpu = torch_gb300.Simulation(p, [1.0], **kw)
+    for _ in range(5):
+        ref.step()
+        gpu.step()
+    assert abs(gpu.time - ref.time) <= 1e-12 * ref.time
+    assert ref.source_integral[-1] > 0
+    np.testing.assert_allclose(gpu.source_integral, ref.source_integral, rtol=1e-9, atol=1e-6)
+    np.testing.assert_allclose(gpu.state, ref.state, rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(gpu.lam, ref.lam, rtol=1e-10, atol=1e-14)

@@ -242,7 +242,10 @@ __device__ __forceinline__ void face_states1(const InstDesc& d, const R* recon, 
 // Wave speeds of the state for the step and the next dt; per tile max |S|
 // over its faces and max(|u| + a) over its cells, integrals, flags.
 template <typename R, bool VARG>
-__global__ void __launch_bounds__(256) waves1d_kernel(StepArgs A) {
+// in_step: the pass inside a step (after the update or the second reaction
+// half step): flags are ORed into the step's, the step's sums are kept;
+// otherwise (bind, re-plan, integrals) the integrals of the state are written.
+__global__ void __launch_bounds__(256) waves1d_kernel(StepArgs A, int in_step) {
   __shared__ double red[40];
   for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
     if (!TFV_IN(45, t, A.ntiles)) continue;
@@ -280,20 +283,26 @@ __global__ void __launch_bounds__(256) waves1d_kernel(StepArgs A) {
       R rho, v, p;
       prim1(u, g, rho, v, p);
       wh = fabs(v) + sound1(rho, p, g);
-      for (int c = 0; c < 3; ++c) sum[c] = (double)u[c];
+      if (!in_step)
+        for (int c = 0; c < 3; ++c) sum[c] = (double)u[c];
       bad = !physical_cell<R, 3>(u);
     }
     const int fl = block_or(bad ? kFlagNonphysical : 0, reinterpret_cast<int*>(red));
     const double mws = (double)block_max(ws, red);
     const double mwh = (double)block_max(wh, red);
-    double sm[3];
-    for (int c = 0; c < 3; ++c) sm[c] = block_sum(sum[c], red);
+    double sm[3] = {0.0, 0.0, 0.0};
+    if (!in_step)  // uniform
+      for (int c = 0; c < 3; ++c) sm[c] = block_sum(sum[c], red);
     if (threadIdx.x == 0) {
       A.t_wmax[(size_t)t * 3 + 0] = mws;
       A.t_wmax[(size_t)t * 3 + 1] = mwh;
       A.t_wmax[(size_t)t * 3 + 2] = 0.0;
-      for (int c = 0; c < 3; ++c) A.t_sum[(size_t)t * 5 + c] = sm[c];
-      A.t_flags[t] = fl;
+      if (in_step) {
+        A.t_flags[t] |= fl;
+      } else {
+        for (int c = 0; c < 3; ++c) A.t_sum[(size_t)t * 5 + c] = sm[c];
+        A.t_flags[t] = fl;
+      }
     }
     __syncthreads();
   }

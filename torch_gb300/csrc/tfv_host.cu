@@ -301,7 +301,8 @@ void layout(tfv_batch* b) {
   o = align_up(o + sizeof(double) * 5 * b->n, 256);
   b->fin_slices = 1;
   for (int i = 0; i < b->n; ++i)
-    b->fin_slices = std::max(b->fin_slices, (b->desc[i].ntiles + 255) / 256);
+    b->fin_slices =
+        std::max(b->fin_slices, (b->desc[i].ntiles + kFinalizeSlice - 1) / kFinalizeSlice);
   b->off_fin = o;  // finalize slice records [n][fin_slices][24] and counters [n]
   o = align_up(o + sizeof(double) * 24 * b->fin_slices * b->n, 256);
   b->off_cnt = o;
@@ -548,17 +549,19 @@ cudaError_t enqueue_step(tfv_batch* b) {
     cudaError_t e = cudaSuccess;
     if (b->reactive) {
       e = launch(b, kOpReact1, 0, 1);
-      if (e == cudaSuccess) e = launch(b, kOpWaves, 1, 1);
+      if (e == cudaSuccess) e = launch(b, kOpWavesStep, 1, 1);
       if (e == cudaSuccess) e = finalize(b, 4, 1);
       if (e == cudaSuccess) e = launch(b, kOpHydro, 1, 2);
       if (e == cudaSuccess) e = launch(b, kOpFallback, 1, 2);
       if (e == cudaSuccess) e = launch(b, kOpSpecies, 1, 2);
       if (e == cudaSuccess) e = launch(b, kOpReact2, 2, 1);
+      // the next dt is planned with gamma of the new composition (SI closure)
+      if (e == cudaSuccess && b->own_gamma) e = launch(b, kOpGamma, 1, 1);
     } else {
       e = launch(b, kOpHydro, 0, 1);
       if (e == cudaSuccess) e = launch(b, kOpFallback, 0, 1);
     }
-    if (e == cudaSuccess) e = launch(b, kOpWaves, 1, 1);
+    if (e == cudaSuccess) e = launch(b, kOpWavesStep, 1, 1);
     if (e == cudaSuccess) e = finalize(b, 0, 1);
     return e;
   }

@@ -33,7 +33,6 @@ namespace tfv {
 
 enum : int { kBcOpen = 0, kBcReflective = 1, kBcPeriodic = 2, kBcInflow = 3 };
 constexpr int kFinalizeThreads = 256;  // threads of a finalize CTA
-constexpr int kFinalizeSlice = 256;    // tiles reduced by one finalize CTA
 constexpr int kPartVals = 23;          // partials per tile: 3 maxima, 15 boundary sums, 5 integrals
 
 // an int carried in a double slot of the finalize records (bit copy)
@@ -1649,6 +1648,7 @@ __global__ void __launch_bounds__(kFinalizeThreads) finalize_kernel(StepArgs A, 
   // result does not depend on which slice finished last) and commits.
   constexpr int NV = kPartVals;
   constexpr int kGroups = kFinalizeThreads / NV;
+  __shared__ double vals[NV][kFinalizeSlice];  // this slice's partials, value-major
   __shared__ double acc[kFinalizeThreads];
   __shared__ double sh_v[NV];
   __shared__ int fred[kFinalizeThreads / 32];
@@ -1668,21 +1668,44 @@ __global__ void __launch_bounds__(kFinalizeThreads) finalize_kernel(StepArgs A, 
   const int t0 = d.tile0 + slice * kFinalizeSlice;
   const int t1 = min(d.tile0 + d.ntiles, t0 + kFinalizeSlice);
   const int j = threadIdx.x;
+  // one tile per thread: every load of the tile's record issued together
   int fl = 0;
-  for (int t = t0 + j; t < t1; t += blockDim.x)
-    if (TFV_IN(32, t, A.ntiles)) fl |= A.t_flags[t];
-  fl = block_or(fl, fred);
+  {
+    const int t = t0 + j;
+    const bool have = j < kFinalizeSlice && t < t1 && TFV_IN(32, t, A.ntiles);
+    double w[3] = {0.0, 0.0, 0.0}, b[15], q[5];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) b[k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) q[k] = 0.0;
+    if (have) {
+      fl = A.t_flags[t];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) w[k] = A.t_wmax[(size_t)t * 3 + k];
+      if (want_s) {
+#pragma unroll
+        for (int k = 0; k < 15; ++k) b[k] = A.t_bsum[(size_t)t * 15 + k];
+      }
+      if (want_i) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) q[k] = A.t_sum[(size_t)t * 5 + k];
+      }
+    }
+    if (j < kFinalizeSlice) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) vals[k][j] = w[k];
+#pragma unroll
+      for (int k = 0; k < 15; ++k) vals[3 + k][j] = b[k];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) vals[18 + k][j] = q[k];
+    }
+  }
+  fl = block_or(fl, fred);  // includes a barrier: vals complete
   double v = 0.0;
   if (j < kGroups * NV) {
     const int k = j % NV, g = j / NV;
-    if (k < 3 || (k < 18 ? want_s : want_i)) {
-      for (int t = t0 + g; t < t1; t += kGroups) {
-        if (!TFV_IN(33, t, A.ntiles)) continue;
-        if (k < 3) v = fmax(v, A.t_wmax[(size_t)t * 3 + k]);
-        else if (k < 18) v += A.t_bsum[(size_t)t * 15 + (k - 3)];
-        else v += A.t_sum[(size_t)t * 5 + (k - 18)];
-      }
-    }
+    const int m = t1 - t0;
+    for (int r = g; r < m; r += kGroups) v = k < 3 ? fmax(v, vals[k][r]) : v + vals[k][r];
   }
   acc[j] = v;
   __syncthreads();
@@ -1704,19 +1727,26 @@ __global__ void __launch_bounds__(kFinalizeThreads) finalize_kernel(StepArgs A, 
     if (!sh_last) return;
     __threadfence();
     const double* base = A.fin_part + (size_t)i * A.fin_slices * (NV + 1);
-    if (j < NV) {
-      double r = __ldcg(base + j);
-      for (int q = 1; q < nslices; ++q) {
-        const double x = __ldcg(base + (size_t)q * (NV + 1) + j);
-        r = j < 3 ? fmax(r, x) : r + x;
+    if (j <= NV) {
+      // slice records in slice order, loads issued eight at a time
+      double r = j == NV ? 0.0 : __ldcg(base + j);
+      int f = j == NV ? __double_bits_as_int(__ldcg(base + NV)) : 0;
+      for (int q0 = 1; q0 < nslices; q0 += 8) {
+        double x[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          x[u] = q0 + u < nslices ? __ldcg(base + (size_t)(q0 + u) * (NV + 1) + j) : 0.0;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (q0 + u >= nslices) break;
+          if (j == NV) f |= __double_bits_as_int(x[u]);
+          else r = j < 3 ? fmax(r, x[u]) : r + x[u];
+        }
       }
-      sh_v[j] = r;
-    } else if (j == 32) {
-      int f = 0;
-      for (int q = 0; q < nslices; ++q) f |= __double_bits_as_int(__ldcg(base + (size_t)q * (NV + 1) + NV));
-      sh_f = f;
-      A.fin_cnt[i] = 0;  // ready for the next launch
+      if (j < NV) sh_v[j] = r;
+      else sh_f = f;
     }
+    if (j == 32) A.fin_cnt[i] = 0;  // ready for the next launch
     __syncthreads();
   }
   const double* sh_w = sh_v;

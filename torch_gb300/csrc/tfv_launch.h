@@ -9,8 +9,10 @@
 
 namespace tfv {
 
+// kOpWavesStep: the 1D chain's wave-speed pass inside a step (keeps the step's
+// source sums and ORs its flags into those of the earlier kernels)
 enum : int { kOpHydro = 0, kOpFallback = 1, kOpWaves = 2, kOpReact1 = 3, kOpReact2 = 4,
-             kOpSpecies = 5, kOpGamma = 6 };
+             kOpSpecies = 5, kOpGamma = 6, kOpWavesStep = 7 };
 
 // lim selects the limiter instantiation of the step kernel (ignored otherwise).
 cudaError_t launch_step1_f64(int op, bool varg, int lim, const StepArgs& A, int grid, int block,

@@ -6,6 +6,7 @@
 namespace tfv {
 
 constexpr int kMaxRing = 3;
+constexpr int kFinalizeSlice = 128;  // tiles reduced by one finalize CTA
 
 // Read-only per-instance description (uploaded once per bind).
 struct InstDesc {
