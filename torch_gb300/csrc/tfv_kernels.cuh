@@ -1483,6 +1483,11 @@ __global__ void __launch_bounds__(256) react_kernel(StepArgs A, int stage) {
     double src[NV];
 #pragma unroll
     for (int c = 0; c < NV; ++c) src[c] = 0.0;
+    // single precision: this thread's column of source terms summed with
+    // compensation (Kahan), converted once; the tile and global sums are FP64
+    R ksum[NV], kcomp[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) ksum[c] = kcomp[c] = R(0);
     int fl = 0;
     if (owner) {
       for (int p = T.p0; p < T.p1; ++p) {
@@ -1499,9 +1504,18 @@ __global__ void __launch_bounds__(256) react_kernel(StepArgs A, int stage) {
         if (stage == 2) {
 #pragma unroll
           for (int c = 0; c < NV; ++c) {
-            const double old = (double)Udst[c * g.cs + off];  // heated state of this step
-            const double start = (double)Ustart[c * g.cs + off];
-            src[c] += ((old - start) + (double)u[c]) - (double)hyd[c];
+            if constexpr (Exact<R>::value) {
+              const double old = Udst[c * g.cs + off];  // heated state of this step
+              const double start = Ustart[c * g.cs + off];
+              src[c] += ((old - start) + u[c]) - hyd[c];
+            } else {
+              const R old = Udst[c * g.cs + off];
+              const R start = Ustart[c * g.cs + off];
+              const R y = (((old - start) + u[c]) - hyd[c]) - kcomp[c];
+              const R t = ksum[c] + y;
+              kcomp[c] = (t - ksum[c]) - y;
+              ksum[c] = t;
+            }
           }
           if (!physical_cell<R, NV>(u)) fl |= kFlagNonphysical;
         }
@@ -1522,7 +1536,10 @@ __global__ void __launch_bounds__(256) react_kernel(StepArgs A, int stage) {
 #pragma unroll
     for (int k = 0; k < DIM; ++k) wm[k] = (double)block_max(owner ? wmax[k] : R(0), red);
 #pragma unroll
-    for (int c = 0; c < NV; ++c) sm[c] = stage == 2 ? block_sum(src[c], red) : 0.0;
+    for (int c = 0; c < NV; ++c) {
+      if constexpr (!Exact<R>::value) src[c] = (double)ksum[c] - (double)kcomp[c];
+      sm[c] = stage == 2 ? block_sum(src[c], red) : 0.0;
+    }
     if (threadIdx.x == 0) {
       for (int k = 0; k < DIM; ++k) A.t_wmax[(size_t)t * 3 + k] = wm[k];
       if (stage == 2) {
