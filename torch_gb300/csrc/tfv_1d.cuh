@@ -244,15 +244,23 @@ __device__ __forceinline__ void face_states1(const InstDesc& d, const R* recon, 
 template <typename R, bool VARG>
 // in_step: the pass inside a step (after the update or the second reaction
 // half step): flags are ORed into the step's, the step's sums are kept;
+// 2: the same, only for instances whose step was redone at first order;
 // otherwise (bind, re-plan, integrals) the integrals of the state are written.
 __global__ void __launch_bounds__(256) waves1d_kernel(StepArgs A, int in_step) {
   __shared__ double red[40];
+  if (in_step == 2) {  // usually no instance took the fallback
+    int any = 0;
+    for (int k = threadIdx.x; k < A.ninst; k += blockDim.x)
+      any |= (A.st[k].status == kReady && A.st[k].fb_word != 0);
+    if (!__syncthreads_or(any)) return;
+  }
   for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
     if (!TFV_IN(45, t, A.ntiles)) continue;
     const Tile T = A.tiles[t];
     if (!TFV_IN(46, T.inst, A.ninst)) continue;
     const InstDesc& d = A.desc[T.inst];
     const InstState& st = A.st[T.inst];
+    if (in_step == 2 && (st.status != kReady || st.fb_word == 0)) continue;  // uniform
     const int n = d.n[0];
     const R* U = (const R*)d.U[(st.cur + A.src_off) % d.nring];
     const R* gam = VARG ? (const R*)d.gam : nullptr;
@@ -308,6 +316,61 @@ __global__ void __launch_bounds__(256) waves1d_kernel(StepArgs A, int in_step) {
   }
 }
 
+// Limited half-step states (left ol, right orr) of a cell with state c0
+// between neighbours cm and cp (python/cfdSolver/torchSolver.py:412-491).
+template <typename R>
+__device__ __forceinline__ void recon1_cells(const InstDesc& d, const InstState& st,
+                                             const R* c0, const R* cm, const R* cp, R g, R* ol,
+                                             R* orr) {
+  R w = R(0);
+  if (d.controller == 0) {  // Sound Speed Controlled
+    R rho, v, p;
+    prim1(c0, g, rho, v, p);
+    const R a = sound1(rho, p, g);
+    const R mach = nan0(fabs(v) / np_max(a, R(kFloor)));
+    w = np_min(np_max((R(1) - mach) / (R(1) + mach), R(-1)), R(1));
+  }
+  R ul[3], ur[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const R delta = R(0.5) * (cp[c] - cm[c]);
+    const R lim = limit1(delta, c0[c] - cm[c], cp[c] - c0[c], w, d.limiter);
+    ul[c] = c0[c] - R(0.5) * lim;
+    ur[c] = c0[c] + R(0.5) * lim;
+  }
+  R fl[3], fr[3];
+  flux1(ul, g, fl);
+  flux1(ur, g, fr);
+  const R k = -R(st.dt / (2.0 * d.h[0]));
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const R dfu = k * (fr[c] - fl[c]);
+    ol[c] = ul[c] + dfu;
+    orr[c] = ur[c] + dfu;
+  }
+  R* outs[2] = {ol, orr};
+  for (int sidx = 0; sidx < 2; ++sidx) {
+    R* s = outs[sidx];
+    const R p = (g - R(1)) * (s[2] - (R(0.5) * (s[1] * s[1])) / np_max(s[0], R(kFloor)));
+    const bool badc = s[0] <= R(kFloor) || p <= R(kFloor) || !isfinite(s[0]) ||
+                      !isfinite(s[1]) || !isfinite(s[2]);
+    if (badc)
+      for (int c = 0; c < 3; ++c) s[c] = c0[c];
+  }
+}
+
+// recon1_cells of cell i read from the state array (one ghost cell by the
+// boundary rule).
+template <typename R>
+__device__ __forceinline__ void recon1(const InstDesc& d, const InstState& st, const R* U,
+                                       const R* gam, int i, R* ol, R* orr) {
+  R c0[3], cm[3], cp[3];
+  cell1(d, U, i, c0);
+  cell1(d, U, i - 1, cm);
+  cell1(d, U, i + 1, cp);
+  recon1_cells<R>(d, st, c0, cm, cp, gamma1(d, gam, i), ol, orr);
+}
+
 // MUSCL reconstruction and half-step predictor per cell
 // (python/cfdSolver/torchSolver.py:412-491).
 template <typename R, bool VARG>
@@ -325,47 +388,8 @@ __global__ void __launch_bounds__(256) recon1d_kernel(StepArgs A) {
     Scratch1D<R> S(d);
     const int i = T.x0 + (int)threadIdx.x;
     if ((int)threadIdx.x >= min(A.tx, n - T.x0)) continue;
-    R c0[3], cm[3], cp[3];
-    cell1(d, U, i, c0);
-    cell1(d, U, i - 1, cm);
-    cell1(d, U, i + 1, cp);
-    const R g = gamma1(d, gam, i);
-    R w = R(0);
-    if (d.controller == 0) {  // Sound Speed Controlled
-      R rho, v, p;
-      prim1(c0, g, rho, v, p);
-      const R a = sound1(rho, p, g);
-      const R mach = nan0(fabs(v) / np_max(a, R(kFloor)));
-      w = np_min(np_max((R(1) - mach) / (R(1) + mach), R(-1)), R(1));
-    }
-    R ul[3], ur[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const R delta = R(0.5) * (cp[c] - cm[c]);
-      const R lim = limit1(delta, c0[c] - cm[c], cp[c] - c0[c], w, d.limiter);
-      ul[c] = c0[c] - R(0.5) * lim;
-      ur[c] = c0[c] + R(0.5) * lim;
-    }
-    R fl[3], fr[3];
-    flux1(ul, g, fl);
-    flux1(ur, g, fr);
-    const R k = -R(st.dt / (2.0 * d.h[0]));
     R ol[3], orr[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const R dfu = k * (fr[c] - fl[c]);
-      ol[c] = ul[c] + dfu;
-      orr[c] = ur[c] + dfu;
-    }
-    R* outs[2] = {ol, orr};
-    for (int sidx = 0; sidx < 2; ++sidx) {
-      R* s = outs[sidx];
-      const R p = (g - R(1)) * (s[2] - (R(0.5) * (s[1] * s[1])) / np_max(s[0], R(kFloor)));
-      const bool badc = s[0] <= R(kFloor) || p <= R(kFloor) || !isfinite(s[0]) ||
-                        !isfinite(s[1]) || !isfinite(s[2]);
-      if (badc)
-        for (int c = 0; c < 3; ++c) s[c] = c0[c];
-    }
+    recon1<R>(d, st, U, gam, i, ol, orr);
     if (!TFV_IN(42, i, n)) continue;
     for (int c = 0; c < 3; ++c) {
       if (!TFV_INSIDE(63, S.recon + (3 + c) * n + i, d.scratch, S.flux + 3 * (n + 1)) ||
@@ -467,6 +491,236 @@ __global__ void __launch_bounds__(256) update1d_kernel(StepArgs A, int first_ord
       for (int c = 0; c < 3; ++c) A.t_bsum[(size_t)t * 15 + c] = sm[c];
       A.t_flags[t] = fl;
       if (fl && !first_order) atomicOr(&st.fb_word, fl);
+    }
+    __syncthreads();
+  }
+}
+
+
+// Face flux at face f (0 <= f <= n) of the current state, evaluated from
+// scratch: the two reconstructed interface states (bc_creator rules at the
+// domain faces, torchSolver.py:494-508), the interface wave speeds
+// (torchSolver.py:283-404) and HLLC with them (torchSolver.py:534-676).
+template <typename R, bool VARG>
+__device__ __forceinline__ void face_flux_direct1(const InstDesc& d, const InstState& st,
+                                                  const R* U, const R* gam, int f, R* F) {
+  const int n = d.n[0];
+  const bool per = d.bc[0] == kBcPeriodic, refl = d.bc[0] == kBcReflective;
+  R ol[3], orr[3], L[3], Rr[3];
+  // left state: the right half-state of cell f-1 (at f == 0: periodic wraps
+  // to cell n-1, otherwise the left half-state of cell 0)
+  const int li = f == 0 ? (per ? n - 1 : 0) : f - 1;
+  const bool l_right = f != 0 || per;
+  recon1<R>(d, st, U, gam, li, ol, orr);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) L[c] = l_right ? orr[c] : ol[c];
+  // right state: the left half-state of cell f (at f == n: periodic wraps to
+  // cell 0, otherwise the right half-state of cell n-1)
+  const int ri = f == n ? (per ? 0 : n - 1) : f;
+  const bool r_left = f != n || per;
+  recon1<R>(d, st, U, gam, ri, ol, orr);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) Rr[c] = r_left ? ol[c] : orr[c];
+  if (f == 0 && refl) L[1] = -L[1];
+  if (f == n && refl) Rr[1] = -Rr[1];
+  R a[3], b[3], s[3];
+  cell1(d, U, f - 1, a);
+  cell1(d, U, f, b);
+  const R gl = gamma1(d, gam, f - 1), gr = gamma1(d, gam, f);
+  waves1(d, a, b, gl, gr, s);
+  hllc1(d, L, Rr, gl, gr, s[0], s[2], F);
+}
+
+// Physical cell of padded index k in [-1, n] (cell1's ghost rule) and
+// whether its momentum is mirrored.
+__device__ __forceinline__ int phys1(const InstDesc& d, int k, bool& flip) {
+  const int n = d.n[0];
+  flip = false;
+  if (k >= 0 && k < n) return k;
+  flip = d.bc[0] == kBcReflective;
+  if (k < 0) return d.bc[0] == kBcPeriodic ? n - 1 : 0;
+  return d.bc[0] == kBcPeriodic ? 0 : n - 1;
+}
+
+// The whole inert 1D step of a tile in one kernel: faces, update, positivity
+// flags, boundary sums, and the next dt's wave speeds of the new state.
+// Shared memory holds the tile's state with a 3-cell halo; every cell is
+// reconstructed once and every face's wave speeds and flux are evaluated once.
+// The CTA also updates the cell on either side of its tile (the neighbouring
+// tile's, or the ghost's source cell at a domain end), so that the interface
+// wave speeds of the new state at its tile faces need no second pass.  Values
+// are the same expressions as in the split kernels (recon1d, update1d,
+// waves1d), so results are identical.  At a periodic domain end the wrapped
+// neighbour lies outside the staged range and is evaluated from global memory.
+template <typename R, bool VARG>
+__global__ void __launch_bounds__(256) step1d_kernel(StepArgs A) {
+  __shared__ double red[40];
+  extern __shared__ __align__(16) unsigned char step1d_smem[];
+  const int W = A.tx + 6;  // staged padded cells x0-3 .. x0+tx+2
+  R* us = reinterpret_cast<R*>(step1d_smem);  // [3][W] state
+  R* gs = us + 3 * W;                          // [W] gamma
+  R* rc = gs + W;                              // [6][W] half-step states (l, r)
+  R* fx = rc + 6 * W;                          // [3][W] flux at the face left of slot k
+  R* un_s = fx + 3 * W;                        // [3][tx + 2] new state of the targets
+  const int TS = A.tx + 2;
+  for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
+    if (!TFV_IN(45, t, A.ntiles)) continue;
+    const Tile T = A.tiles[t];
+    if (!TFV_IN(46, T.inst, A.ninst)) continue;
+    const InstDesc& d = A.desc[T.inst];
+    InstState& st = A.st[T.inst];
+    if (st.status != kReady) continue;  // uniform
+    const int n = d.n[0];
+    const R* U = (const R*)d.U[(st.cur + A.src_off) % d.nring];
+    R* Un = (R*)d.U[(st.cur + A.dst_off) % d.nring];
+    const R* gam = VARG ? (const R*)d.gam : nullptr;
+    const int ax = min(A.tx, n - T.x0);
+    const int x0 = T.x0;
+    const bool per = d.bc[0] == kBcPeriodic, refl = d.bc[0] == kBcReflective;
+    // slot k <-> padded cell x0 - 3 + k
+    for (int k = threadIdx.x; k < ax + 6; k += blockDim.x) {
+      const int pk = x0 - 3 + k;
+      if (pk < -1 || pk > n) continue;
+      R u[3];
+      cell1(d, U, pk, u);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) us[c * W + k] = u[c];
+      gs[k] = gamma1(d, gam, pk);
+    }
+    __syncthreads();
+    // half-step states of the cells x0-2 .. x0+ax+1 inside the domain
+    for (int k = 1 + threadIdx.x; k < ax + 5; k += blockDim.x) {
+      const int i = x0 - 3 + k;
+      if (i < 0 || i >= n) continue;
+      R c0[3], cm[3], cp[3], ol[3], orr[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        c0[c] = us[c * W + k];
+        cm[c] = us[c * W + k - 1];
+        cp[c] = us[c * W + k + 1];
+      }
+      recon1_cells<R>(d, st, c0, cm, cp, gs[k], ol, orr);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        rc[c * W + k] = ol[c];
+        rc[(3 + c) * W + k] = orr[c];
+      }
+    }
+    __syncthreads();
+    // faces x0-1 .. x0+ax+1 inside [0, n]; face f lies left of slot k = f - x0 + 3
+    for (int k = 2 + threadIdx.x; k < ax + 5; k += blockDim.x) {
+      const int f = x0 - 3 + k;
+      if (f < 0 || f > n) continue;
+      R L[3], Rr[3], ol[3], orr[3];
+      if (f == 0 && per) {  // wraps to cell n-1: outside the staged range
+        recon1<R>(d, st, U, gam, n - 1, ol, orr);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) L[c] = orr[c];
+      } else {
+        // f == 0: left half-state of cell 0 (slot k); else right half of f-1
+#pragma unroll
+        for (int c = 0; c < 3; ++c) L[c] = f == 0 ? rc[c * W + k] : rc[(3 + c) * W + k - 1];
+      }
+      if (f == n && per) {  // wraps to cell 0
+        recon1<R>(d, st, U, gam, 0, ol, orr);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Rr[c] = ol[c];
+      } else {
+        // f == n: right half-state of cell n-1 (slot k-1); else left half of f
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Rr[c] = f == n ? rc[(3 + c) * W + k - 1] : rc[c * W + k];
+      }
+      if (f == 0 && refl) L[1] = -L[1];
+      if (f == n && refl) Rr[1] = -Rr[1];
+      R a[3], b[3], w3[3], F[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        a[c] = us[c * W + k - 1];
+        b[c] = us[c * W + k];
+      }
+      waves1(d, a, b, gs[k - 1], gs[k], w3);
+      hllc1(d, L, Rr, gs[k - 1], gs[k], w3[0], w3[2], F);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) fx[c * W + k] = F[c];
+    }
+    __syncthreads();
+    // targets: slot q <-> padded x0 + q - 1, q in [0, ax + 1]
+    const R kk = -R(st.coef_full[0]);
+    double bsum[3] = {0.0, 0.0, 0.0};
+    bool bad = false;
+    for (int q = threadIdx.x; q < ax + 2; q += blockDim.x) {
+      bool flip;
+      const int j = phys1(d, x0 + q - 1, flip);
+      R Fm[3], Fp[3], u[3];
+      if (j >= x0 - 1 && j <= x0 + ax) {  // the cell and its faces are staged
+        const int k = j - x0 + 3;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          Fm[c] = fx[c * W + k];
+          Fp[c] = fx[c * W + k + 1];
+          u[c] = us[c * W + k];
+        }
+      } else {  // periodic wrap at a domain end
+        face_flux_direct1<R, VARG>(d, st, U, gam, j, Fm);
+        face_flux_direct1<R, VARG>(d, st, U, gam, j + 1, Fp);
+        cell1(d, U, j, u);
+      }
+      R un[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) un[c] = u[c] + kk * (Fp[c] - Fm[c]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) un_s[c * TS + q] = un[c];
+      if (q >= 1 && q <= ax) {  // a cell of this tile
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          if (!TFV_IN(44, j, n) || !TFV_OUTSIDE(65, Un + c * n + j, A.ws_lo, A.ws_hi)) continue;
+          Un[c * n + j] = un[c];
+          if (j == 0) bsum[c] -= (double)Fm[c];
+          if (j == n - 1) bsum[c] += (double)Fp[c];
+        }
+        if (!physical_cell<R, 3>(un)) bad = true;
+      }
+    }
+    __syncthreads();
+    // the next dt: interface wave speeds and |u| + a of the new state
+    R ws = R(0), wh = R(0);
+    const int nf = ax + (x0 + ax == n ? 1 : 0);  // faces x0 .. x0+ax-1 (+ face n)
+    for (int s = threadIdx.x; s < nf; s += blockDim.x) {
+      const int f = x0 + s;
+      bool fl_l, fl_r;
+      phys1(d, f - 1, fl_l);
+      phys1(d, f, fl_r);
+      R L[3], Rr[3], w3[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        L[c] = un_s[c * TS + s];
+        Rr[c] = un_s[c * TS + s + 1];
+      }
+      if (fl_l) L[1] = -L[1];
+      if (fl_r) Rr[1] = -Rr[1];
+      waves1(d, L, Rr, gamma1(d, gam, f - 1), gamma1(d, gam, f), w3);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) ws = fmax(ws, fabs(w3[k]));
+      if (s < ax) {
+        R rho, v, p;
+        const R g = gamma1(d, gam, f);
+        R uc[3] = {un_s[0 * TS + s + 1], un_s[1 * TS + s + 1], un_s[2 * TS + s + 1]};
+        prim1(uc, g, rho, v, p);
+        wh = fmax(wh, fabs(v) + sound1(rho, p, g));
+      }
+    }
+    const int fl = block_or(bad ? kFlagNonphysical : 0, reinterpret_cast<int*>(red));
+    const double mws = (double)block_max(ws, red);
+    const double mwh = (double)block_max(wh, red);
+    double sm[3];
+    for (int c = 0; c < 3; ++c) sm[c] = block_sum(bsum[c], red);
+    if (threadIdx.x == 0) {
+      A.t_wmax[(size_t)t * 3 + 0] = mws;
+      A.t_wmax[(size_t)t * 3 + 1] = mwh;
+      A.t_wmax[(size_t)t * 3 + 2] = 0.0;
+      for (int c = 0; c < 3; ++c) A.t_bsum[(size_t)t * 15 + c] = sm[c];
+      A.t_flags[t] = fl;
+      if (fl) atomicOr(&st.fb_word, fl);
     }
     __syncthreads();
   }

@@ -557,11 +557,14 @@ cudaError_t enqueue_step(tfv_batch* b) {
       if (e == cudaSuccess) e = launch(b, kOpReact2, 2, 1);
       // the next dt is planned with gamma of the new composition (SI closure)
       if (e == cudaSuccess && b->own_gamma) e = launch(b, kOpGamma, 1, 1);
+      if (e == cudaSuccess) e = launch(b, kOpWavesStep, 1, 1);
     } else {
-      e = launch(b, kOpHydro, 0, 1);
+      // fused step (faces, update, next-dt wave speeds); the first-order
+      // fallback and its wave pass run only for flagged instances
+      e = launch(b, kOpStep1d, 0, 1);
       if (e == cudaSuccess) e = launch(b, kOpFallback, 0, 1);
+      if (e == cudaSuccess) e = launch(b, kOpWavesFallback, 1, 1);
     }
-    if (e == cudaSuccess) e = launch(b, kOpWavesStep, 1, 1);
     if (e == cudaSuccess) e = finalize(b, 0, 1);
     return e;
   }

@@ -10,9 +10,12 @@
 namespace tfv {
 
 // kOpWavesStep: the 1D chain's wave-speed pass inside a step (keeps the step's
-// source sums and ORs its flags into those of the earlier kernels)
+// source sums and ORs its flags into those of the earlier kernels);
+// kOpStep1d: the fused inert 1D step; kOpWavesFallback: the wave-speed pass
+// for the instances whose step was redone at first order
 enum : int { kOpHydro = 0, kOpFallback = 1, kOpWaves = 2, kOpReact1 = 3, kOpReact2 = 4,
-             kOpSpecies = 5, kOpGamma = 6, kOpWavesStep = 7 };
+             kOpSpecies = 5, kOpGamma = 6, kOpWavesStep = 7,
+             kOpStep1d = 8, kOpWavesFallback = 9 };
 
 // lim selects the limiter instantiation of the step kernel (ignored otherwise).
 cudaError_t launch_step1_f64(int op, bool varg, int lim, const StepArgs& A, int grid, int block,
