@@ -920,7 +920,7 @@ int tfv_batch_replan(tfv_batch* b) {
   int r = check_bound(b);
   if (r) return r;
   if (b->own_gamma) TFV_CUDA(launch(b, kOpGamma, 0, 0));
-  TFV_CUDA(launch(b, kOpWaves, 0, 0));
+  TFV_CUDA(launch(b, kOpWavesPlan, 0, 0));
   TFV_CUDA(finalize(b, 1, 0));
   return TFV_OK;
 }
@@ -954,7 +954,7 @@ int tfv_batch_restore(tfv_batch* b, const tfv_report* reports) {
   TFV_CUDA(cudaMemcpyAsync(b->ws + b->off_st, b->st.data(), sizeof(InstState) * b->n,
                            cudaMemcpyHostToDevice, b->stream));
   if (b->own_gamma) TFV_CUDA(launch(b, kOpGamma, 0, 0));
-  TFV_CUDA(launch(b, kOpWaves, 0, 0));
+  TFV_CUDA(launch(b, kOpWavesPlan, 0, 0));
   TFV_CUDA(finalize(b, 1, 0));
   TFV_CUDA(cudaStreamSynchronize(b->stream));
   return TFV_OK;

@@ -1199,7 +1199,9 @@ __global__ void __launch_bounds__(256) fallback_kernel(StepArgs A) {
 // Wave-speed maxima of the current state (initial / re-planned dt).
 // --------------------------------------------------------------------------
 template <typename R, int DIM, bool VARG>
-__global__ void __launch_bounds__(256) waves_kernel(StepArgs A) {
+// sums: also the integrals of the state (bind, integrals); re-planning needs
+// only the wave maxima and flags.
+__global__ void __launch_bounds__(256) waves_kernel(StepArgs A, int sums) {
   constexpr int NV = DIM + 2;
   __shared__ double red[40];
   for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
@@ -1230,9 +1232,10 @@ __global__ void __launch_bounds__(256) waves_kernel(StepArgs A) {
         if (!TFV_IN(27, off, g.cs)) continue;
         R u[NV];
 #pragma unroll
-        for (int c = 0; c < NV; ++c) {
-          u[c] = U[c * g.cs + off];
-          sum[c] += (double)u[c];
+        for (int c = 0; c < NV; ++c) u[c] = U[c * g.cs + off];
+        if (sums) {
+#pragma unroll
+          for (int c = 0; c < NV; ++c) sum[c] += (double)u[c];
         }
         const R gc = VARG ? gam[off] : R(d.gamma);
         if (!physical_cell<R, NV>(u)) bad = true;
@@ -1247,10 +1250,11 @@ __global__ void __launch_bounds__(256) waves_kernel(StepArgs A) {
 #pragma unroll
     for (int k = 0; k < DIM; ++k) wm[k] = (double)block_max(owner ? wmax[k] : R(0), red);
 #pragma unroll
-    for (int c = 0; c < NV; ++c) sm[c] = block_sum(sum[c], red);
+    for (int c = 0; c < NV; ++c) sm[c] = sums ? block_sum(sum[c], red) : 0.0;  // uniform
     if (threadIdx.x == 0) {
       for (int k = 0; k < DIM; ++k) A.t_wmax[(size_t)t * 3 + k] = wm[k];
-      for (int c = 0; c < NV; ++c) A.t_sum[(size_t)t * 5 + c] = sm[c];
+      if (sums)
+        for (int c = 0; c < NV; ++c) A.t_sum[(size_t)t * 5 + c] = sm[c];
       A.t_flags[t] = fl;
     }
     __syncthreads();

@@ -12,10 +12,11 @@ namespace tfv {
 // kOpWavesStep: the 1D chain's wave-speed pass inside a step (keeps the step's
 // source sums and ORs its flags into those of the earlier kernels);
 // kOpStep1d: the fused inert 1D step; kOpWavesFallback: the wave-speed pass
-// for the instances whose step was redone at first order
+// for the instances whose step was redone at first order; kOpWavesPlan: wave
+// maxima and flags of the current state without its integrals (re-planning)
 enum : int { kOpHydro = 0, kOpFallback = 1, kOpWaves = 2, kOpReact1 = 3, kOpReact2 = 4,
              kOpSpecies = 5, kOpGamma = 6, kOpWavesStep = 7,
-             kOpStep1d = 8, kOpWavesFallback = 9 };
+             kOpStep1d = 8, kOpWavesFallback = 9, kOpWavesPlan = 10 };
 
 // lim selects the limiter instantiation of the step kernel (ignored otherwise).
 cudaError_t launch_step1_f64(int op, bool varg, int lim, const StepArgs& A, int grid, int block,
