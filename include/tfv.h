@@ -171,11 +171,14 @@ int tfv_batch_report(tfv_batch* b, tfv_report* out);
 int tfv_batch_integrals(tfv_batch* b, double* out);
 
 /* Carry instances that already advanced into this (freshly bound) batch:
- * for each i with reports[i].steps > 0 or reports[i].time > 0, restore time,
- * steps, integrals, fallback counters and a terminal status, then re-plan dt
- * from the current states.  The caller passes each instance's current state
- * as ring buffer 0 at bind.  Used to re-batch grids when requests join or
- * leave (no reference counterpart: TORCH sessions are never batched). */
+ * for each i whose report is not all-zero (steps > 0, time > 0 or a nonzero
+ * initial mass integral), restore time, steps, integrals, fallback counters
+ * and a terminal status, then re-plan dt from the current states; zero
+ * reports leave their instance as bound.  The caller passes each instance's
+ * current state as ring buffer 0 at bind.  Used to re-batch grids when
+ * requests join or leave and to resume a checkpointed session with its exact
+ * counters and balances (python/cfdSolver/torchIO.py:233-391 restores the
+ * same attributes on the reference's session). */
 int tfv_batch_restore(tfv_batch* b, const tfv_report* reports);
 
 /* Re-plan after the caller wrote new values into the current buffers

@@ -218,10 +218,9 @@ def chemistry_cases(R, rng):
     np.savez_compressed(OUT / "chemistry.npz", **out)
 
 
-def session_cases(R, rng):
-    """Multi-step Simulation.step() trajectories (state, time, integrals)."""
+def session_setups(R):
+    """The session cases of sessions.npz and checkpoint.npz, freshly built."""
     S = R.torchSession.Simulation
-    out = {}
     cases = {}
     cases["s2d_explosion"] = S.preset("2d_explosion", [24, 20], t_end=0.05,
                                       limiter="VanLeer")
@@ -254,6 +253,13 @@ def session_cases(R, rng):
     p1r[:, 20:] = np.array([0.5, 0.0, 101325.0])[:, None]
     cases["s1d_reactive_znd"] = S(p1r, [1.0], t_end=2e-6, reactive=True,
                                   kinetic_model="znd")
+    return cases
+
+
+def session_cases(R, rng):
+    """Multi-step Simulation.step() trajectories (state, time, integrals)."""
+    out = {}
+    cases = session_setups(R)
     for name, s in cases.items():
         out[f"{name}_state0"] = s.state.copy()
         if s.lam is not None:
@@ -274,6 +280,81 @@ def session_cases(R, rng):
         out[f"{name}_source"] = s.source_integral
         out[f"{name}_initial"] = s.initial_integral
     np.savez_compressed(OUT / "sessions.npz", **out)
+
+
+class _RecordingHDF5(types.ModuleType):
+    """Stand-in for h5py (absent here) under the reference's checkpoint writer
+    and reader: datasets are kept as NumPy arrays in an .npz container, so the
+    reference's own write_checkpoint / read_checkpoint run unchanged."""
+
+    class File:
+        def __init__(self, path, mode="r"):
+            self.path, self.mode = Path(path), mode
+            self.data = {}
+            if mode == "r":
+                with np.load(self.path) as z:
+                    self.data = {k.replace("|", "/"): z[k] for k in z.files}
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *exc):
+            if self.mode == "w" and exc[0] is None:
+                with open(self.path, "wb") as f:
+                    np.savez(f, **{k.replace("/", "|"): v for k, v in self.data.items()})
+
+        def create_dataset(self, name, data, **options):
+            self.data[name] = np.array(data)
+
+        def flush(self):
+            pass
+
+        def __getitem__(self, name):
+            if name in self.data:
+                return self.data[name]
+            prefix = name + "/"
+            members = [k[len(prefix):] for k in self.data if k.startswith(prefix)]
+            if not members:
+                raise KeyError(name)
+            return members
+
+
+def checkpoint_cases(R):
+    """Reference checkpoints taken after 4 steps (write_checkpoint's metadata
+    bytes and datasets), accepted by the reference's read_checkpoint, and the
+    reference's state after 4 more steps from there."""
+    import tempfile
+    sys.modules["h5py"] = _RecordingHDF5("h5py")
+    io = importlib.import_module("cfdSolver.torchIO")
+    cases = session_setups(R)
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name in ("s3d_explosion", "s3d_open_albada", "s2d_explosion", "s1d_sod",
+                     "s3d_ignition_znd", "s3d_ignition_arr", "s2d_reactive",
+                     "s1d_reactive_znd"):
+            s = cases[name]
+            # a later end time so that all 8 steps run (the session reads it each step)
+            s.config["t_end"] = 1e-3 if s.config["reactive"] else 1.0
+            for _ in range(4):
+                s.step()
+            path = Path(tmp) / (name + ".h5")
+            io.write_checkpoint(path, s)
+            with _RecordingHDF5.File(path) as f:
+                for key, value in f.data.items():
+                    out[f"{name}|{key}"] = value
+            back = io.read_checkpoint(path)
+            assert back.steps == s.steps == 4 and np.array_equal(back.state, s.state)
+            for _ in range(4):
+                back.step()
+            out[f"{name}|final/state"] = back.state
+            for key in ("lam", "beta"):
+                if getattr(back, key) is not None:
+                    out[f"{name}|final/{key}"] = getattr(back, key)
+            out[f"{name}|final/scalars"] = np.array([back.time, back.steps])
+            out[f"{name}|final/initial"] = back.initial_integral
+            out[f"{name}|final/boundary"] = back.boundary_integral
+            out[f"{name}|final/source"] = back.source_integral
+    np.savez_compressed(OUT / "checkpoint.npz", **out)
 
 
 def large_cfl_case(R):
@@ -334,6 +415,9 @@ def exact_riemann_cases():
 
 def main():
     R = load_reference()
+    if sys.argv[1:] == ["checkpoint"]:  # regenerate checkpoint.npz alone
+        checkpoint_cases(R)
+        return
     rng = np.random.default_rng(20261203)
     hllc_cases(R, rng)
     step3d_cases(R, rng)
@@ -342,6 +426,7 @@ def main():
     session_cases(R, rng)
     large_cfl_case(R)
     exact_riemann_cases()
+    checkpoint_cases(R)
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

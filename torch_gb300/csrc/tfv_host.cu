@@ -934,7 +934,7 @@ int tfv_batch_restore(tfv_batch* b, const tfv_report* reports) {
   TFV_CUDA(cudaStreamSynchronize(b->stream));
   for (int i = 0; i < b->n; ++i) {
     const tfv_report& o = reports[i];
-    if (!(o.steps > 0 || o.time > 0)) continue;
+    if (!(o.steps > 0 || o.time > 0 || o.initial_integral[0] != 0)) continue;
     InstState& s = b->st[i];
     s.time = o.time;
     s.steps = o.steps;

@@ -82,6 +82,40 @@ def make_config(dim, counts, lengths, boundaries, *, t_end, cfl, gamma, limiter,
     return cfg
 
 
+def validate_config(c, strict_cfl=True):
+    """Session configuration checks (torchSession.py:190-254), Cartesian."""
+    dim = c["dimension"]
+    if not isinstance(dim, (int, np.integer)) or dim not in (1, 2, 3) or isinstance(dim, bool):
+        raise ValueError("Invalid dimension")
+    for key in ("counts_xyz", "lengths_xyz", "boundaries_xyz"):
+        if len(c[key]) != dim:
+            raise ValueError("Incomplete mesh/boundary metadata")
+    for length, n in zip(c["lengths_xyz"], c["counts_xyz"]):
+        _validate_grid(length, n, c["cfl"], c["t_end"], strict_cfl)
+    origin = np.asarray(c.get("origins_xyz", [0.0] * dim), dtype=float)
+    if origin.shape != (dim,) or not np.isfinite(origin).all():  # torchGeometry.py:45-55
+        raise ValueError("One finite origin per logical coordinate is required")
+    if not np.isfinite(c["gamma"]) or c["gamma"] <= 1:
+        raise ValueError("gamma must be finite and greater than one")
+    if c["limiter"] not in LIMITERS or c["kinetic_model"] not in ("arrhenius", "znd"):
+        raise ValueError("Unknown limiter or chemistry model")
+    if (not isinstance(c["max_steps"], (int, np.integer)) or isinstance(c["max_steps"], bool)
+            or c["max_steps"] < 1):
+        raise ValueError("Invalid maximum steps")
+    for axis, boundary in enumerate(c["boundaries_xyz"]):
+        if boundary not in ("Open", "Reflective", "Periodic") and not (
+                dim == 2 and axis == 1 and boundary == "Inflow"):
+            raise ValueError("Unsupported session boundary")
+    if c["controller"] not in _lib.CONTROLLERS or c["variant"] not in _lib.VARIANTS or \
+            c["wavespeed"] not in _lib.WAVESPEEDS:
+        raise ValueError("Unknown solver option")
+    if dim == 2 and "Inflow" in c["boundaries_xyz"]:
+        inlet = np.asarray(c["inlet_primitive"])
+        if (inlet.shape != (4,) or not np.isfinite(inlet).all() or inlet[0] <= 0
+                or inlet[3] <= 0 or inlet[2] < 0):
+            raise ValueError("Invalid inlet primitives")
+
+
 def _dtype(precision):
     if precision not in ("fp64", "fp32"):
         raise ValueError("precision must be 'fp64' or 'fp32'")
@@ -143,6 +177,13 @@ class _Engine:
 
     def advance(self, nsteps):
         _lib.check(self.lib.tfv_batch_advance(self.handle, int(nsteps)))
+
+    def restore(self, reports):
+        """Carry time, steps, integrals and fallback counters of an earlier run
+        into this freshly bound engine (its current states are ring slot 0)."""
+        arr = (_lib.Report * self.n)(*reports)
+        _lib.check(self.lib.tfv_batch_restore(self.handle, arr))
+        self.refresh()
 
     def profile(self, nsteps):
         """Milliseconds (step kernel, fallback, finalize) summed over nsteps."""
@@ -275,34 +316,8 @@ class Simulation:
             return (4.5 - lam) / (3.5 - lam)
         return self.config["gamma"]
 
-    # -- validation (torchSession.py:190-254) -------------------------------
     def _validate_config(self):
-        c = self.config
-        dim = c["dimension"]
-        for key in ("counts_xyz", "lengths_xyz", "boundaries_xyz"):
-            if len(c[key]) != dim:
-                raise ValueError("Incomplete mesh/boundary metadata")
-        for length, n in zip(c["lengths_xyz"], c["counts_xyz"]):
-            _validate_grid(length, n, c["cfl"], c["t_end"], self._strict_cfl)
-        if not np.isfinite(c["gamma"]) or c["gamma"] <= 1:
-            raise ValueError("gamma must be finite and greater than one")
-        if c["limiter"] not in LIMITERS or c["kinetic_model"] not in ("arrhenius", "znd"):
-            raise ValueError("Unknown limiter or chemistry model")
-        if (not isinstance(c["max_steps"], (int, np.integer)) or isinstance(c["max_steps"], bool)
-                or c["max_steps"] < 1):
-            raise ValueError("Invalid maximum steps")
-        for axis, boundary in enumerate(c["boundaries_xyz"]):
-            if boundary not in ("Open", "Reflective", "Periodic") and not (
-                    dim == 2 and axis == 1 and boundary == "Inflow"):
-                raise ValueError("Unsupported session boundary")
-        if c["controller"] not in _lib.CONTROLLERS or c["variant"] not in _lib.VARIANTS or \
-                c["wavespeed"] not in _lib.WAVESPEEDS:
-            raise ValueError("Unknown solver option")
-        if dim == 2 and "Inflow" in c["boundaries_xyz"]:
-            inlet = np.asarray(c["inlet_primitive"])
-            if (inlet.shape != (4,) or not np.isfinite(inlet).all() or inlet[0] <= 0
-                    or inlet[3] <= 0 or inlet[2] < 0):
-                raise ValueError("Invalid inlet primitives")
+        validate_config(self.config, self._strict_cfl)
 
     # -- workers: the GPU replaces the CPU flux pool (torchExecution.py) ----
     @property
@@ -453,19 +468,104 @@ class Simulation:
 
     def run(self, *, step_limit=None, checkpoint=None, checkpoint_every=0, output_prefix=None,
             output_every=1, formats=("vtk", "xdmf"), chunk=64):
+        """Advance to t_end or by `step_limit` steps (torchSession.py:578-632).
+        With `checkpoint`, a checkpoint is written whenever the step count
+        reaches a multiple of `checkpoint_every` and once at the end; steps
+        are enqueued in chunks that stop at those multiples, so no numerical
+        step is shortened.  Field output (VTK/XDMF) is the reference's host IO
+        and is not produced here."""
         for value in (step_limit, checkpoint_every, output_every):
             if value is not None and (not isinstance(value, int) or value < 0):
                 raise ValueError("Step intervals must be nonnegative integers")
-        if checkpoint or output_prefix:
-            raise NotImplementedError("checkpoint and field output need the reference's torchIO")
+        if checkpoint_every and not checkpoint:
+            raise ValueError("checkpoint_every requires a checkpoint destination")
+        if output_prefix and output_every < 1:
+            raise ValueError("output_every must be positive")
+        if output_prefix:
+            raise NotImplementedError("VTK/XDMF field output is written by the reference's torchIO")
         remaining = step_limit
         while not self.completed and (remaining is None or remaining > 0):
             self._raise_pending()
             k = chunk if remaining is None else min(chunk, remaining)
+            if checkpoint and checkpoint_every:
+                k = min(k, checkpoint_every - self.steps % checkpoint_every)
             before = self.steps
             self._engine.advance(k)
             self._engine.refresh()
             if remaining is not None:
                 remaining -= self.steps - before
             self._raise_pending()
+            if (checkpoint and checkpoint_every and self.steps != before
+                    and self.steps % checkpoint_every == 0):
+                self.save(checkpoint)
+        if checkpoint:
+            self.save(checkpoint)
         return self
+
+    # -- checkpoint interchange (torchSession.py:634-651) ----------------------
+    def save(self, path):
+        """Write a TORCH checkpoint (schema 2) of this session; the reference's
+        read_checkpoint accepts it."""
+        from . import checkpoint
+        return checkpoint.write(path, self)
+
+    @classmethod
+    def load(cls, path, *, t_end=None, **options):
+        """Resume a TORCH checkpoint on the GPU, optionally with a later end
+        time (torchSession.py:640-651).  `options` are the GPU extensions
+        accepted by `from_session`."""
+        from . import checkpoint
+        snap = checkpoint.read(path)
+        if t_end is not None:
+            if not np.isfinite(t_end) or t_end < snap.time:
+                raise ValueError("New end time must be finite and not precede checkpoint")
+            snap.config["t_end"] = t_end
+        return cls.from_session(snap, **options)
+
+    @classmethod
+    def from_session(cls, session, **options):
+        """A GPU session that continues `session`: any object with the
+        reference session's attributes (config, state, lam, beta, time, steps,
+        initial/boundary/source integrals, run_id), such as the reference's
+        own Simulation or a checkpoint Snapshot.  The conservative state and
+        composition are taken exactly; `options` adds GPU extensions
+        (precision, strict_cfl, chemistry, tile, graph_steps, device)."""
+        c = session.config
+        if c.get("geometry", "cartesian") != "cartesian" or "face_boundaries" in c:
+            raise NotImplementedError(
+                "metric/face-boundary sessions run on the reference's CPU kernel")
+        state = np.array(session.state, dtype=float)
+        reactive = bool(c["reactive"])
+        lam = np.array(session.lam, dtype=float) if reactive else None
+        znd = reactive and c["kinetic_model"] == "znd"
+        beta = np.array(session.beta, dtype=float) if znd else None
+        closure = dict(options.get("chemistry") or {}).get("closure", "si")
+        gamma = (4.5 - lam) / (3.5 - lam) if reactive and closure == "si" else c["gamma"]
+        primitive = state.copy()
+        primitive[1:-1] /= state[0]
+        primitive[-1] = (gamma - 1) * (state[-1] - 0.5 * np.sum(state[1:-1] ** 2, axis=0)
+                                       / state[0])
+        kw = dict(t_end=c["t_end"], cfl=c["cfl"], gamma=c["gamma"],
+                  boundaries=list(c["boundaries_xyz"]), limiter=c["limiter"], reactive=reactive,
+                  kinetic_model=c["kinetic_model"], lambda_init=lam, beta_init=beta,
+                  inlet_primitive=c.get("inlet_primitive"),
+                  controller=c.get("controller", "Sound Speed Controlled"),
+                  variant=c.get("variant", "Variante 1 - Original"),
+                  wavespeed=c.get("wavespeed", "Pressure Based"), max_steps=c["max_steps"],
+                  origins=c.get("origins_xyz"))
+        kw.update(options)
+        sim = cls(primitive, list(c["lengths_xyz"]), **kw)
+        sim.state = state  # exact conservative values, not a round trip through primitives
+        report = _lib.Report()
+        report.time = float(session.time)
+        report.steps = int(session.steps)
+        for field, name in ((report.initial_integral, "initial_integral"),
+                            (report.boundary_integral, "boundary_integral"),
+                            (report.source_integral, "source_integral")):
+            for k, v in enumerate(np.asarray(getattr(session, name), dtype=float)):
+                field[k] = v
+        report.fallback_steps = int(getattr(session, "fallback_steps", 0))
+        report.status = _lib.READY
+        sim._engine.restore([report])
+        sim.run_id = getattr(session, "run_id", None) or sim.run_id
+        return sim
