@@ -361,9 +361,8 @@ def main():
     ap.add_argument("--skip-reactive", action="store_true")
     ap.add_argument("--skip-served", action="store_true")
     ap.add_argument("--served-count", type=int, default=16)
-    ap.add_argument("--e2e-streams", type=int, default=1,
-                    help="copy streams per host<->device transfer in the end-to-end loop "
-                         "(measured on GB300: more streams do not raise the copy rate)")
+    ap.add_argument("--e2e-sessions", type=int, default=3,
+                    help="independent sessions stepped end to end on their own streams")
     ap.add_argument("--graph-steps", type=int, default=10,
                     help="steps captured per CUDA graph in the headline run")
     args = ap.parse_args()
@@ -426,42 +425,59 @@ def main():
     hbm, peak_kind = peaks()
     achieved = BYTES_PER_CELL["fp32"] * cells / (step_kernel_ms * 1e-3) / 1e9
 
-    # end to end: host state in pinned memory, H2D + step + D2H every step
-    eng.refresh()
-    cur = eng.current()
-    host_in = torch.empty(cur.shape, dtype=cur.dtype, pin_memory=True)
-    host_out = torch.empty_like(host_in, pin_memory=True)
-    host_in.copy_(cur)
+    # end to end: host state in pinned memory, H2D + step + D2H every step.
+    # Independent sessions (requests) are pipelined: uploads go through one
+    # stream and downloads through another (each direction in issue order,
+    # the GB300's host link carries both at once), each session steps on its
+    # own stream, and events order a session's upload after its previous
+    # download (both use its current state slot).
+    sessions = [sim] + [torch_gb300.Simulation(prim, [1, 1, 1], precision="fp32", tile=tile, **kw)
+                        for _ in range(max(1, args.e2e_sessions) - 1)]
+    lanes = []
+    for s_i in sessions:
+        e_i = s_i._engine
+        e_i.refresh()
+        cur = e_i.current()
+        host_in = torch.empty(cur.shape, dtype=cur.dtype, pin_memory=True)
+        host_out = torch.empty_like(host_in, pin_memory=True)
+        host_in.copy_(cur)
+        lanes.append(dict(sim=s_i, eng=e_i, host_in=host_in, host_out=host_out,
+                          c=e_i.reports[0].current, down=None))
     torch.cuda.synchronize()
     e2e_steps = max(3, min(args.steps, 10))
+    main = torch.cuda.current_stream()
+    up, down = torch.cuda.Stream(), torch.cuda.Stream()
     s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
-    s2.record(stream)
-    c = eng.reports[0].current  # ring index of the current state; each step flips it
-    # each copy is split into chunks on separate streams so that several copy
-    # engines move it in parallel; events keep the step ordered after them
-    lanes = [torch.cuda.Stream() for _ in range(max(1, args.e2e_streams))]
-
-    def chunked(dst, src):
-        d, s = dst.view(-1).chunk(len(lanes)), src.view(-1).chunk(len(lanes))
-        for lane, dd, ss in zip(lanes, d, s):
-            lane.wait_stream(stream)
-            with torch.cuda.stream(lane):
-                dd.copy_(ss, non_blocking=True)
+    s2.record(main)
+    up.wait_stream(main)
+    down.wait_stream(main)
+    for lane in lanes:
+        lane["eng"].stream.wait_stream(main)
+    for _ in range(e2e_steps):
         for lane in lanes:
-            stream.wait_stream(lane)
-
-    with torch.cuda.stream(stream):
-        for _ in range(e2e_steps):
-            chunked(eng.rings[0][c], host_in)
-            eng.replan_async()
-            sim.advance(1)
-            c = (c + 1) % eng.nring
-            chunked(host_out, eng.rings[0][c])
-    e2.record(stream)
+            e_i, c = lane["eng"], lane["c"]
+            if lane["down"] is not None:
+                up.wait_event(lane["down"])  # the previous result has left this slot
+            with torch.cuda.stream(up):
+                e_i.rings[0][c].copy_(lane["host_in"], non_blocking=True)
+            e_i.stream.wait_stream(up)
+            with torch.cuda.stream(e_i.stream):
+                e_i.replan_async()
+                lane["sim"].advance(1)
+            c = (c + 1) % e_i.nring  # ring index of the new current state
+            down.wait_stream(e_i.stream)
+            with torch.cuda.stream(down):
+                lane["host_out"].copy_(e_i.rings[0][c], non_blocking=True)
+                lane["down"] = torch.cuda.Event()
+                lane["down"].record(down)
+            lane["c"] = c
+    main.wait_stream(down)
+    e2.record(main)
     barrier()
-    e2e_ms = s2.elapsed_time(e2) / e2e_steps
+    e2e_ms = s2.elapsed_time(e2) / (e2e_steps * len(lanes))
     e2e_ms = max_over_ranks(e2e_ms, dist, "cuda")
+    cur = eng.current()
     nbytes = cur.numel() * cur.element_size()
 
     # FP64 plain path on the same workload (a few steps) and the FP32 error
@@ -529,7 +545,9 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": world * cells / (e2e_ms * 1e-3), "unit": UNIT,
                     "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                    "ms_per_step": e2e_ms, "copy_streams": args.e2e_streams},
+                    "ms_per_step": e2e_ms, "sessions_in_flight": len(lanes),
+                    "note": "each session-step uploads its state from pinned host memory, "
+                            "re-plans dt, steps and downloads the result"},
             "gpu_launches": 3 * args.steps,
             "graph_steps": args.graph_steps,
             "clocks": clocks.summary(),

@@ -238,6 +238,91 @@ int tfv_hydro_step_static(const tfv_config* cfg, int32_t precision, const void* 
                           void* state_out, const void* gamma_cells, double dt, void* fx,
                           void* fy, void* fz, int32_t* used_fallback, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Metric / face-boundary sessions: TORCH's second finite-volume scheme
+ * (python/cfdSolver/torchFiniteVolume.py:1-276), used by the reference session
+ * for cylindrical, annular and spherical grids and for any grid with per-face
+ * boundaries (torchSession.py:303-308, 523-576): MUSCL reconstruction of
+ * primitives, area-weighted Rusanov fluxes, geometric source terms, SSPRK2
+ * with a first-order retry, up to 20 dt halvings, Strang-split chemistry.
+ * ------------------------------------------------------------------------- */
+
+/* geometries (python/cfdSolver/torchGeometry.py:9) */
+enum { TFV_GEO_CARTESIAN = 0, TFV_GEO_CYLINDRICAL = 1, TFV_GEO_ANNULAR = 2, TFV_GEO_SPHERICAL = 3 };
+
+/* face boundary kinds (python/cfdSolver/torchBoundaries.py:8-15) */
+enum {
+  TFV_FACE_OUTFLOW = 0,
+  TFV_FACE_WALL = 1,
+  TFV_FACE_PERIODIC = 2,
+  TFV_FACE_INFLOW = 3,
+  TFV_FACE_PRESSURE_OUTLET = 4,
+  TFV_FACE_STAGNATION_INLET = 5
+};
+
+/* one face (torchBoundaries.py:18-171, normalised): faces are ordered
+ * x_min, x_max, y_min, y_max, z_min, z_max */
+typedef struct tfv_metric_face {
+  int32_t type;              /* TFV_FACE_* */
+  int32_t has_backflow;      /* pressure outlet: primitive[] holds the backflow state */
+  double primitive[5];       /* inflow state, or the pressure outlet's backflow state */
+  double lambda_, beta;      /* fractions carried in (default 1) */
+  double pressure;           /* pressure outlet */
+  double total_pressure, total_temperature, gas_constant;  /* stagnation inlet */
+} tfv_metric_face;
+
+typedef struct tfv_metric_config {
+  int32_t dim;
+  int32_t n[3];              /* cells along x, y, z */
+  double lengths[3];
+  int32_t geometry;          /* TFV_GEO_* */
+  int32_t limiter;           /* TFV_VANLEER ... */
+  int32_t reactive;
+  int32_t model;             /* TFV_ARRHENIUS / TFV_ZND (SI closure) */
+  double cfl, gamma, t_end;
+  int64_t max_steps;
+  double q, ea, a;           /* chemistry constants */
+  tfv_metric_face faces[6];
+} tfv_metric_config;
+
+typedef struct tfv_metric tfv_metric;
+
+/* Number of geometry factors tfv_metric_create expects: the volume factors
+ * of each axis (n[a] values, x first), then for each direction d the face
+ * factors of each axis a (n[a] + 1 values when a == d, else n[a]).  Volumes
+ * and face areas are their outer products, multiplied x, then y, then z
+ * (torchGeometry.py:95-170). */
+int64_t tfv_metric_factor_count(const tfv_metric_config* cfg);
+
+/* Validate the configuration and lay out the workspace
+ * (Simulation.__init__ metric branch, torchSession.py:24-158). */
+int tfv_metric_create(int32_t precision, const tfv_metric_config* cfg, const double* factors,
+                      tfv_metric** out);
+int tfv_metric_workspace_size(tfv_metric* m, size_t* bytes);
+
+/* Attach the workspace (256-byte aligned) and the two state slots (and
+ * lambda / beta slots of reactive sessions); slot 0 holds the initial state.
+ * Computes the initial integral. */
+int tfv_metric_bind(tfv_metric* m, void* workspace, void* const* states, void* const* lams,
+                    void* const* betas, void* stream);
+
+/* Up to nsteps transactional steps (torchSession.py:523-576); stops at t_end.
+ * A failed step leaves the current state, time and balances unchanged:
+ * TFV_EINVAL for boundary or chemistry input the reference rejects with
+ * ValueError, TFV_ENUMERIC for stall / maximum steps / positivity. */
+int tfv_metric_advance(tfv_metric* m, int32_t nsteps);
+int tfv_metric_report(tfv_metric* m, tfv_report* out);
+
+/* Integral of the current state (torchSession.py:284-294) into out[dim+2]. */
+int tfv_metric_integrals(tfv_metric* m, double* out);
+
+/* Carry time, steps and balances of an earlier run (checkpoint resume). */
+int tfv_metric_restore(tfv_metric* m, const tfv_report* r);
+
+/* Make slot 0 or 1 the current one (after the caller rewrote a state). */
+int tfv_metric_set_current(tfv_metric* m, int32_t slot);
+int tfv_metric_destroy(tfv_metric* m);
+
 #ifdef __cplusplus
 }
 #endif

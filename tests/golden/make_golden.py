@@ -12,6 +12,7 @@ uses small seeded inputs.  Outputs go to ``tests/golden/*.npz`` next to this
 script and are committed; tests read them without the reference.
 """
 
+import json
 import os
 import sys
 import types
@@ -357,6 +358,130 @@ def checkpoint_cases(R):
     np.savez_compressed(OUT / "checkpoint.npz", **out)
 
 
+def metric_setups(R):
+    """Metric / face-boundary sessions: every geometry and dimension with the
+    inflow / pressure-outlet faces of python/tests/testGeometry.py:27-65, and
+    walls at radial origins and poles, a stagnation inlet, a full periodic
+    azimuth, all limiters, reactive shells."""
+    S = R.torchSession.Simulation
+    limiters = ("VanLeer", "Albada", "MINBEE", "Superbee", "Unos")
+    cases = {}
+
+    def centres(origin, lengths, counts):
+        c = [o + (np.arange(n) + 0.5) * l / n for o, l, n in zip(origin, lengths, counts)]
+        return np.meshgrid(*c[::-1], indexing="ij")[::-1]
+
+    k = 0
+    for dim in (1, 2, 3):
+        for geometry in ("cartesian", "cylindrical", "annular", "spherical"):
+            for reactive in (False, True):
+                if reactive and geometry in ("cartesian", "cylindrical"):
+                    continue
+                counts = [12, 6, 4][:dim]
+                origin = [0.4, 0.3, 0.2][:dim] if geometry != "cartesian" else [0.1] * dim
+                lengths = [0.8, 0.6, 0.4][:dim]
+                g = centres(origin, lengths, counts)
+                p = np.ones((dim + 2, *counts[::-1]))
+                p[0] = 1 + 0.05 * np.sin(3 * g[0])
+                if dim > 1:
+                    p[0] += 0.03 * np.cos(2 * g[1])
+                if dim == 3:
+                    p[0] += 0.01 * g[2]
+                p[1:-1] = 0.15
+                p[-1] = np.where(g[0] < 0.8, 1e6, 101325.0) if reactive else 1.0 + 0.3 * (g[0] < 0.8)
+                pr = 101325.0 if reactive else 1.0
+                faces = {
+                    "x_min": {"type": "inflow",
+                              "primitive": [1.0, 0.15] + [0.15] * (dim - 1) + [pr]},
+                    "x_max": {"type": "pressure_outlet", "pressure": pr,
+                              "backflow": [1.0, -0.1] + [0.0] * (dim - 1) + [pr]},
+                }
+                name = f"m{dim}d_{geometry}" + ("_reactive" if reactive else "")
+                model = "znd" if reactive and dim != 2 else "arrhenius"
+                cases[name] = S(p, lengths, geometry=geometry, origins=origin,
+                                t_end=2e-5 if reactive else 0.025, reactive=reactive,
+                                kinetic_model=model, limiter=limiters[k % 5],
+                                face_boundaries=faces)
+                k += 1
+    # radial origin (default wall) and both spherical poles, at rest with a pressure bump
+    for dim, geometry in ((2, "cylindrical"), (2, "spherical"), (1, "spherical")):
+        counts = [10, 8][:dim]
+        lengths = [1.0, np.pi][:dim]
+        g = centres([0.0] * dim, lengths, counts)
+        p = np.ones((dim + 2, *counts[::-1]))
+        p[1:-1] = 0.0
+        p[-1] = 1.0 + 0.5 * np.exp(-10 * (g[0] - 0.5) ** 2)
+        cases[f"m{dim}d_{geometry}_origin"] = S(p, lengths, geometry=geometry,
+                                                 origins=[0.0] * dim, t_end=0.05,
+                                                 limiter="Superbee")
+    # full periodic azimuth, stagnation inlet inside, subsonic outlet outside
+    counts = [12, 16]
+    g = centres([0.5, 0.0], [1.0, 2 * np.pi], counts)
+    p = np.ones((4, *counts[::-1]))
+    p[1] = 0.1
+    p[2] = 0.2 * np.sin(g[1])
+    p[3] = 1.0 - 0.05 * g[0]
+    cases["m2d_annular_stagnation"] = S(
+        p, [1.0, 2 * np.pi], geometry="annular", origins=[0.5, 0.0], t_end=0.05,
+        limiter="Albada", boundaries=["Open", "Periodic"],
+        face_boundaries={"x_min": {"type": "stagnation_inlet", "total_pressure": 1.2,
+                                   "total_temperature": 1.2 / 287.0},
+                         "x_max": {"type": "pressure_outlet", "pressure": 0.9}})
+    # Cartesian 3D with a wall, periodic pair and outflow faces
+    counts = [8, 6, 5]
+    g = centres([0.0] * 3, [1.0] * 3, counts)
+    p = np.ones((5, *counts[::-1]))
+    p[0] += 0.2 * np.sin(2 * np.pi * g[1])
+    p[1] = 0.3
+    p[2] = -0.2
+    p[3] = 0.1
+    p[4] = 1 + 0.5 * (g[0] < 0.5)
+    cases["m3d_cartesian_faces"] = S(
+        p, [1.0] * 3, t_end=0.05, limiter="Unos", boundaries=["Open", "Periodic", "Open"],
+        face_boundaries={"x_min": "wall", "z_max": "wall"})
+    return cases
+
+
+def metric_cases(R):
+    """Reference metric / face-boundary sessions: one-stage right-hand sides
+    (second and first order) and cfl_dt at the initial state, then a few
+    complete steps (state, composition, times, balances)."""
+    fvm = importlib.import_module("cfdSolver.torchFiniteVolume")
+    out = {}
+    for name, s in metric_setups(R).items():
+        c = s.config
+        out[f"{name}|config"] = np.frombuffer(json.dumps(c).encode(), dtype=np.uint8)
+        out[f"{name}|state0"] = s.state.copy()
+        fractions = [q for q in (s.lam, s.beta) if q is not None]
+        for q, key in zip(fractions, ("lam0", "beta0")):
+            out[f"{name}|{key}"] = q.copy()
+        out[f"{name}|dt0"] = np.array([fvm.cfl_dt(s.state, s.lam, c, s.metrics)])
+        for order in (0, 1):
+            change, species, outward, source = fvm.rhs(s.state, fractions, c, s.metrics,
+                                                       first_order=bool(order))
+            out[f"{name}|rhs{order}/change"] = change
+            for j, sp in enumerate(species):
+                out[f"{name}|rhs{order}/species{j}"] = sp
+            out[f"{name}|rhs{order}/outward"] = outward
+            out[f"{name}|rhs{order}/source"] = source
+        times = []
+        for _ in range(4):
+            if s.completed:
+                break
+            s.step()
+            times.append(s.time)
+        out[f"{name}|times"] = np.array(times)
+        out[f"{name}|state"] = s.state
+        if s.lam is not None:
+            out[f"{name}|lam"] = s.lam
+        if s.beta is not None:
+            out[f"{name}|beta"] = s.beta
+        out[f"{name}|initial"] = s.initial_integral
+        out[f"{name}|boundary"] = s.boundary_integral
+        out[f"{name}|source"] = s.source_integral
+    np.savez_compressed(OUT / "metric.npz", **out)
+
+
 def large_cfl_case(R):
     """2D explosion at CFL 0.8 (rejected by Simulation): dt from the session
     formula, step function called directly, 12 steps on a 40x40 grid."""
@@ -418,6 +543,9 @@ def main():
     if sys.argv[1:] == ["checkpoint"]:  # regenerate checkpoint.npz alone
         checkpoint_cases(R)
         return
+    if sys.argv[1:] == ["metric"]:  # regenerate metric.npz alone
+        metric_cases(R)
+        return
     rng = np.random.default_rng(20261203)
     hllc_cases(R, rng)
     step3d_cases(R, rng)
@@ -427,6 +555,7 @@ def main():
     large_cfl_case(R)
     exact_riemann_cases()
     checkpoint_cases(R)
+    metric_cases(R)
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

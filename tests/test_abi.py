@@ -78,7 +78,8 @@ def test_precision_units_share_no_mergeable_symbols():
     from torch_gb300 import build
     build.build()
     objs = {name: build.BUILD / (Path(name).stem + ".o") for name in build.UNITS}
-    f64 = _weak_symbols(objs["tfv_f64.cu"])
-    for unit in ("tfv_f32_2d.cu", "tfv_f32_3d.cu"):
-        shared = f64 & _weak_symbols(objs[unit])
-        assert not shared, sorted(shared)[:5]
+    for double_unit in ("tfv_f64.cu", "tfv_metric_f64.cu"):
+        f64 = _weak_symbols(objs[double_unit])
+        for unit in ("tfv_f32_2d.cu", "tfv_f32_3d.cu", "tfv_metric_f32.cu"):
+            shared = f64 & _weak_symbols(objs[unit])
+            assert not shared, (double_unit, unit, sorted(shared)[:5])

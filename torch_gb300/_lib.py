@@ -63,8 +63,43 @@ class Report(C.Structure):
     ]
 
 
+GEOMETRIES = {"cartesian": 0, "cylindrical": 1, "annular": 2, "spherical": 3}
+FACE_TYPES = {"outflow": 0, "wall": 1, "periodic": 2, "inflow": 3, "pressure_outlet": 4,
+              "stagnation_inlet": 5}
+
+
+class MetricFace(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32), ("has_backflow", C.c_int32), ("primitive", C.c_double * 5),
+        ("lambda_", C.c_double), ("beta", C.c_double), ("pressure", C.c_double),
+        ("total_pressure", C.c_double), ("total_temperature", C.c_double),
+        ("gas_constant", C.c_double),
+    ]
+
+
+class MetricConfig(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32), ("n", C.c_int32 * 3), ("lengths", C.c_double * 3),
+        ("geometry", C.c_int32), ("limiter", C.c_int32), ("reactive", C.c_int32),
+        ("model", C.c_int32), ("cfl", C.c_double), ("gamma", C.c_double), ("t_end", C.c_double),
+        ("max_steps", C.c_int64), ("q", C.c_double), ("ea", C.c_double), ("a", C.c_double),
+        ("faces", MetricFace * 6),
+    ]
+
+
 _VP = C.c_void_p
 _SIGS = {
+    "tfv_metric_factor_count": ([C.POINTER(MetricConfig)], C.c_int64),
+    "tfv_metric_create": ([C.c_int32, C.POINTER(MetricConfig), C.POINTER(C.c_double),
+                           C.POINTER(_VP)], C.c_int),
+    "tfv_metric_workspace_size": ([_VP, C.POINTER(C.c_size_t)], C.c_int),
+    "tfv_metric_bind": ([_VP, _VP, C.POINTER(_VP), C.POINTER(_VP), C.POINTER(_VP), _VP], C.c_int),
+    "tfv_metric_advance": ([_VP, C.c_int32], C.c_int),
+    "tfv_metric_report": ([_VP, C.POINTER(Report)], C.c_int),
+    "tfv_metric_integrals": ([_VP, C.POINTER(C.c_double)], C.c_int),
+    "tfv_metric_restore": ([_VP, C.POINTER(Report)], C.c_int),
+    "tfv_metric_set_current": ([_VP, C.c_int32], C.c_int),
+    "tfv_metric_destroy": ([_VP], C.c_int),
     "tfv_version": ([], C.c_char_p),
     "tfv_last_error": ([], C.c_char_p),
     "tfv_batch_create": ([C.c_int32, C.c_int32, C.c_int32, C.POINTER(Config), C.POINTER(Tile),

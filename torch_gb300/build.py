@@ -33,6 +33,9 @@ UNITS = {
     "tfv_f32_3d.cu": F32,
     "tfv_f32_2d.cu": F32,
     "tfv_host.cu": [],
+    "tfv_metric_f64.cu": ["-fmad=false"],
+    "tfv_metric_f32.cu": F32,
+    "tfv_metric_host.cu": [],
 }
 
 

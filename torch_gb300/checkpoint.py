@@ -110,10 +110,20 @@ class Snapshot:
 
     @property
     def integral(self):
-        """Cell sums times the cell volume (torchSession.py:284-294)."""
+        """Cell sums times the cell volume, or the sum of each cell times its
+        own volume on metric grids (torchSession.py:284-294)."""
         c = self.config
+        dim = c["dimension"]
+        if c.get("geometry", "cartesian") != "cartesian":
+            from .metric import factors
+            volumes = np.ones(tuple(c["counts_xyz"][::-1]))
+            for d, f in enumerate(factors(c)[0]):
+                shape = [1] * dim
+                shape[dim - 1 - d] = len(f)
+                volumes *= np.asarray(f).reshape(shape)
+            return (self.state * volumes[None]).reshape(dim + 2, -1).sum(axis=1)
         spacing = np.array(c["lengths_xyz"]) / c["counts_xyz"]
-        return self.state.reshape(c["dimension"] + 2, -1).sum(axis=1) * np.prod(spacing)
+        return self.state.reshape(dim + 2, -1).sum(axis=1) * np.prod(spacing)
 
     @property
     def completed(self):
@@ -147,8 +157,6 @@ def parse(datasets):
             raise ValueError("Schema 1 only supports legacy Cartesian configurations")
         if version[0] == 2 and meta.get("geometry") != config.get("geometry", "cartesian"):
             raise ValueError("Checkpoint geometry/configuration mismatch")
-        if config.get("geometry", "cartesian") != "cartesian" or "face_boundaries" in config:
-            raise ValueError("Only Cartesian checkpoints resume on the GPU session")
         for key in ("counts_xyz", "lengths_xyz", "boundaries_xyz", "origins_xyz"):
             if key in config:
                 config[key] = list(np.atleast_1d(config[key]))

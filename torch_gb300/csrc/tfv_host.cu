@@ -46,6 +46,11 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 }  // namespace
 
+namespace tfv {
+int host_fail(int code, const char* msg) { return fail(code, msg); }
+int host_cuda_fail(cudaError_t e, const char* where) { return cuda_fail(e, where); }
+}  // namespace tfv
+
 struct tfv_batch {
   int dim = 0, precision = 0, n = 0;
   std::vector<tfv_config> cfg;

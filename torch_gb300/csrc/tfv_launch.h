@@ -48,4 +48,8 @@ int occupancy3_f32(bool varg, int tx, int ty);
 cudaError_t launch_finalize(const StepArgs& A, int mode, int fp32, double* integrals_out,
                             cudaStream_t s);
 
+// Error text of the C ABI (tfv_last_error), shared by the host units.
+int host_fail(int code, const char* msg);
+int host_cuda_fail(cudaError_t e, const char* where);
+
 }  // namespace tfv

@@ -1,11 +1,14 @@
-"""GPU drop-in for TORCH's Cartesian ``Simulation`` session.
+"""GPU drop-in for TORCH's ``Simulation`` session.
 
-Mirrors python/cfdSolver/torchSession.py:19-694 for Cartesian uniform grids
-(the ``uses_metric_kernel == False`` branch of ``Simulation.step``): same
-constructor keywords, state layout ``(dim+2, nz, ny, nx)`` x fastest,
-properties, transactional ``step()`` and exception types.  The state lives on
-the GPU; ``state``, ``lam`` and ``beta`` materialise as host float64 arrays on
-access so that host-side consumers (checkpoint writers, plots) keep working.
+Mirrors python/cfdSolver/torchSession.py:19-694: same constructor keywords,
+state layout ``(dim+2, nz, ny, nx)`` x fastest, properties, transactional
+``step()``, checkpoints and exception types.  Cartesian grids run the
+MUSCL-Hancock + HLLC engine (``tfv_batch_*``); cylindrical, annular and
+spherical grids and grids with per-face boundaries run the metric engine
+(``tfv_metric_*``, torch_gb300/metric.py), as the reference's
+``uses_metric_kernel`` selects.  The state lives on the GPU; ``state``,
+``lam`` and ``beta`` materialise as host float64 arrays on access so that
+host-side consumers (checkpoint writers, plots) keep working.
 
 Extensions (off by default): ``precision="fp32"`` runs the bulk step in FP32
 with FP64 time and conservation sums; ``strict_cfl=False`` accepts CFL > 0.5
@@ -20,6 +23,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from . import metric
 
 LIMITERS = ("VanLeer", "Albada", "MINBEE", "Superbee", "Unos")
 DEFAULT_INLET = [1.0, 0.0, 100.0, 101325.0]
@@ -92,9 +96,13 @@ def validate_config(c, strict_cfl=True):
             raise ValueError("Incomplete mesh/boundary metadata")
     for length, n in zip(c["lengths_xyz"], c["counts_xyz"]):
         _validate_grid(length, n, c["cfl"], c["t_end"], strict_cfl)
-    origin = np.asarray(c.get("origins_xyz", [0.0] * dim), dtype=float)
-    if origin.shape != (dim,) or not np.isfinite(origin).all():  # torchGeometry.py:45-55
-        raise ValueError("One finite origin per logical coordinate is required")
+    metric.validate_geometry(c)
+    if c.get("geometry", "cartesian") != "cartesian" or "face_boundaries" in c:
+        c["face_boundaries"] = metric.normalize_faces(c, c.get("face_boundaries"))
+        if (c["controller"], c["variant"], c["wavespeed"]) != (
+                "Sound Speed Controlled", "Variante 1 - Original", "Pressure Based"):
+            raise ValueError("Metric/face sessions use MUSCL-Rusanov/SSPRK2; legacy HLLC "
+                             "switches are unsupported")
     if not np.isfinite(c["gamma"]) or c["gamma"] <= 1:
         raise ValueError("gamma must be finite and greater than one")
     if c["limiter"] not in LIMITERS or c["kinetic_model"] not in ("arrhenius", "znd"):
@@ -255,13 +263,13 @@ class Simulation:
         if len(lengths) != dim:
             raise ValueError("Lengths must be in x,y,z order, one per active axis")
         boundaries = list(boundaries) if boundaries is not None else ["Open"] * dim
-        if geometry != "cartesian" or face_boundaries is not None:
-            raise NotImplementedError(
-                "metric/face-boundary sessions run on the reference's CPU kernel")
+        uses_metric = geometry != "cartesian" or face_boundaries is not None
         chem = dict(chemistry or {})
         closure = chem.pop("closure", "si")
         if closure not in _lib.CLOSURES:
             raise ValueError("Unknown chemistry closure")
+        if uses_metric and closure != "si":
+            raise ValueError("Metric/face sessions use the SI chemistry closure")
         self.config = dict(
             dimension=dim, counts_xyz=counts, lengths_xyz=lengths, boundaries_xyz=boundaries,
             t_end=t_end, cfl=cfl, gamma=gamma, limiter=limiter, reactive=bool(reactive),
@@ -270,6 +278,9 @@ class Simulation:
             controller=controller, variant=variant, wavespeed=wavespeed, max_steps=max_steps,
             geometry=geometry, origins_xyz=(list(np.atleast_1d(origins)) if origins is not None
                                             else [0.0] * dim))
+        if uses_metric:  # walls implied at a radial origin and at poles (torchSession.py:89-121)
+            self.config["face_boundaries"] = metric.normalize_faces(
+                self.config, metric.default_face_spec(self.config, face_boundaries))
         self._strict_cfl = strict_cfl
         self._closure = closure
         self._chem = chem
@@ -288,14 +299,19 @@ class Simulation:
         self.precision = precision
         self.device = torch.device(device) if device is not None else torch.device(
             "cuda", torch.cuda.current_device())
-        cfg = make_config(dim, counts, lengths, boundaries, t_end=t_end, cfl=cfl, gamma=gamma,
-                          limiter=limiter, max_steps=max_steps, reactive=reactive,
-                          kinetic_model=kinetic_model, closure=closure, chemistry=chem,
-                          inlet_primitive=inlet_primitive, controller=controller,
-                          variant=variant, wavespeed=wavespeed)
-        self._engine = _Engine(dim, precision, [cfg], [state], self.device, tile=tile,
-                               lams=None if lam0 is None else [lam0],
-                               betas=None if beta0 is None else [beta0])
+        if uses_metric:
+            self._engine = metric.MetricEngine(self.config, self.config["face_boundaries"], state,
+                                               lam0, beta0, precision, self.device,
+                                               dict(SI_CHEMISTRY, **chem))
+        else:
+            cfg = make_config(dim, counts, lengths, boundaries, t_end=t_end, cfl=cfl, gamma=gamma,
+                              limiter=limiter, max_steps=max_steps, reactive=reactive,
+                              kinetic_model=kinetic_model, closure=closure, chemistry=chem,
+                              inlet_primitive=inlet_primitive, controller=controller,
+                              variant=variant, wavespeed=wavespeed)
+            self._engine = _Engine(dim, precision, [cfg], [state], self.device, tile=tile,
+                                   lams=None if lam0 is None else [lam0],
+                                   betas=None if beta0 is None else [beta0])
         if graph_steps:
             self._engine.use_graph(graph_steps)
         self.run_id = str(uuid.uuid4())
@@ -416,7 +432,9 @@ class Simulation:
 
     @property
     def uses_metric_kernel(self):
-        return False
+        """torchSession.py:303-308"""
+        return self.config.get("geometry", "cartesian") != "cartesian" or \
+            "face_boundaries" in self.config
 
     @property
     def primitive(self):
@@ -531,9 +549,6 @@ class Simulation:
         composition are taken exactly; `options` adds GPU extensions
         (precision, strict_cfl, chemistry, tile, graph_steps, device)."""
         c = session.config
-        if c.get("geometry", "cartesian") != "cartesian" or "face_boundaries" in c:
-            raise NotImplementedError(
-                "metric/face-boundary sessions run on the reference's CPU kernel")
         state = np.array(session.state, dtype=float)
         reactive = bool(c["reactive"])
         lam = np.array(session.lam, dtype=float) if reactive else None
@@ -552,7 +567,8 @@ class Simulation:
                   controller=c.get("controller", "Sound Speed Controlled"),
                   variant=c.get("variant", "Variante 1 - Original"),
                   wavespeed=c.get("wavespeed", "Pressure Based"), max_steps=c["max_steps"],
-                  origins=c.get("origins_xyz"))
+                  origins=c.get("origins_xyz"), geometry=c.get("geometry", "cartesian"),
+                  face_boundaries=c.get("face_boundaries"))
         kw.update(options)
         sim = cls(primitive, list(c["lengths_xyz"]), **kw)
         sim.state = state  # exact conservative values, not a round trip through primitives
