@@ -361,7 +361,7 @@ def main():
     ap.add_argument("--skip-reactive", action="store_true")
     ap.add_argument("--skip-served", action="store_true")
     ap.add_argument("--served-count", type=int, default=16)
-    ap.add_argument("--e2e-sessions", type=int, default=3,
+    ap.add_argument("--e2e-sessions", type=int, default=4,
                     help="independent sessions stepped end to end on their own streams")
     ap.add_argument("--graph-steps", type=int, default=10,
                     help="steps captured per CUDA graph in the headline run")

@@ -323,6 +323,15 @@ int tfv_metric_restore(tfv_metric* m, const tfv_report* r);
 int tfv_metric_set_current(tfv_metric* m, int32_t slot);
 int tfv_metric_destroy(tfv_metric* m);
 
+/* Rusanov fluxes of n independent faces (python/cfdSolver/torchFlux.py:80-122,
+ * rusanov_flux / rusanov_flux_grid; the adaptive solver's leaf-face batches,
+ * torchAdaptive.py:115-135).  left, right: [nv][n] primitive face states
+ * (rho, velocities, p) with nv = dim + 2 in 3..5; gl, gr: [n]; out: [nv][n]
+ * fluxes; direction: the normal velocity row minus one. */
+int tfv_rusanov_flux(int32_t precision, int32_t nv, int64_t n, int32_t direction,
+                     const void* left, const void* right, const void* gl, const void* gr,
+                     void* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

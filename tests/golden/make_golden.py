@@ -482,6 +482,64 @@ def metric_cases(R):
     np.savez_compressed(OUT / "metric.npz", **out)
 
 
+def rusanov_cases(R):
+    """The reference's rusanov_flux (torchFlux.py:80-99) on seeded random
+    faces in 1D/2D/3D along every direction with per-face gamma, and the
+    leaf-face batches an adaptive session hands to it (torchAdaptive.py:
+    115-135), recorded from two steps of a refined 2D cylindrical blast."""
+    flux = importlib.import_module("cfdSolver.torchFlux")
+    rng = np.random.default_rng(11)
+    out = {}
+    for dim in (1, 2, 3):
+        nv = dim + 2
+        for d in range(dim):
+            n = 256
+            left = np.empty((nv, n))
+            right = np.empty((nv, n))
+            for a in (left, right):
+                a[0] = 10 ** rng.uniform(-2, 1, n)
+                a[1:-1] = rng.uniform(-3, 3, (dim, n))
+                a[-1] = 10 ** rng.uniform(-2, 2, n)
+            gl = rng.uniform(1.1, 1.67, n)
+            gr = rng.uniform(1.1, 1.67, n)
+            key = f"random{dim}d_dir{d}"
+            out[f"{key}|left"], out[f"{key}|right"] = left, right
+            out[f"{key}|gl"], out[f"{key}|gr"] = gl, gr
+            out[f"{key}|flux"] = flux.rusanov_flux(left, right, gl, gr, d)
+    adaptive = importlib.import_module("cfdSolver.torchAdaptive")
+    S = R.torchSession.Simulation
+    counts = [12, 8]
+    p = np.ones((4, *counts[::-1]))
+    p[1:-1] = 0.0
+    r = 0.2 + (np.arange(counts[0]) + 0.5) / counts[0]
+    p[-1] = np.where(r < 0.5, 4.0, 1.0)[None, :]
+    s = S(p, [1.0, 1.0], geometry="cylindrical", origins=[0.2, 0.0], t_end=0.05)
+    a = s.to_adaptive(max_level=2)
+    a.regrid(refine=a.mesh.centers[:, 0] < 0.7, coarsen=False)
+    calls = []
+    original = adaptive.rusanov
+
+    def recording(left, right, gl, gr, k):
+        value = original(left, right, gl, gr, k)
+        calls.append((left.copy(), right.copy(), np.array(gl, copy=True),
+                      np.array(gr, copy=True), k, value))
+        return value
+
+    adaptive.rusanov = recording
+    try:
+        for _ in range(2):
+            a.step()
+    finally:
+        adaptive.rusanov = original
+    for i, (left, right, gl, gr, k, value) in enumerate(calls[:4]):
+        key = f"amr{i}"
+        out[f"{key}|left"], out[f"{key}|right"] = left, right
+        out[f"{key}|gl"], out[f"{key}|gr"] = gl, gr
+        out[f"{key}|dir"] = np.array([k])
+        out[f"{key}|flux"] = value
+    np.savez_compressed(OUT / "rusanov.npz", **out)
+
+
 def large_cfl_case(R):
     """2D explosion at CFL 0.8 (rejected by Simulation): dt from the session
     formula, step function called directly, 12 steps on a 40x40 grid."""
@@ -546,6 +604,9 @@ def main():
     if sys.argv[1:] == ["metric"]:  # regenerate metric.npz alone
         metric_cases(R)
         return
+    if sys.argv[1:] == ["rusanov"]:  # regenerate rusanov.npz alone
+        rusanov_cases(R)
+        return
     rng = np.random.default_rng(20261203)
     hllc_cases(R, rng)
     step3d_cases(R, rng)
@@ -556,6 +617,7 @@ def main():
     exact_riemann_cases()
     checkpoint_cases(R)
     metric_cases(R)
+    rusanov_cases(R)
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -8,8 +8,10 @@ mirrors the reference's session and step-function interfaces.
 
 from . import _lib  # noqa: F401
 from .session import Simulation  # noqa: F401
-from .stepfn import (hllc_flux, hllc_flux_grid, muscl_hancock_step_2d,  # noqa: F401
+from .stepfn import (hllc_flux, hllc_flux_grid, rusanov_flux, rusanov_flux_grid,  # noqa: F401
+                     muscl_hancock_step_2d,
                      muscl_hancock_step_3d)
 
-__all__ = ["Simulation", "hllc_flux", "hllc_flux_grid", "muscl_hancock_step_2d",
+__all__ = ["Simulation", "hllc_flux", "hllc_flux_grid", "rusanov_flux", "rusanov_flux_grid",
+           "muscl_hancock_step_2d",
            "muscl_hancock_step_3d"]

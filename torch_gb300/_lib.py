@@ -100,6 +100,8 @@ _SIGS = {
     "tfv_metric_restore": ([_VP, C.POINTER(Report)], C.c_int),
     "tfv_metric_set_current": ([_VP, C.c_int32], C.c_int),
     "tfv_metric_destroy": ([_VP], C.c_int),
+    "tfv_rusanov_flux": ([C.c_int32, C.c_int32, C.c_int64, C.c_int32, _VP, _VP, _VP, _VP, _VP,
+                          _VP], C.c_int),
     "tfv_version": ([], C.c_char_p),
     "tfv_last_error": ([], C.c_char_p),
     "tfv_batch_create": ([C.c_int32, C.c_int32, C.c_int32, C.POINTER(Config), C.POINTER(Tile),

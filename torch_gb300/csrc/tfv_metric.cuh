@@ -657,7 +657,52 @@ __global__ void __launch_bounds__(kMThreads) metric_integral_kernel(MArgs<R> A) 
   }
 }
 
-// -- 8. block partials -> totals, in block order -------------------------------
+// -- 8. stateless Rusanov over a list of faces ---------------------------------
+// rows of the face states: rho, velocities (NV - 2), p; fluxes in the same
+// component order (python/cfdSolver/torchFlux.py:80-99).
+template <typename R, int NV>
+__global__ void __launch_bounds__(kMThreads) rusanov_faces_kernel(
+    int64_t n, int dir, const R* __restrict__ L, const R* __restrict__ Rt,
+    const R* __restrict__ GL, const R* __restrict__ GR, R* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    R left[NV], right[NV], ul[NV], ur[NV], fl[NV], fr[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      left[v] = L[v * n + i];
+      right[v] = Rt[v * n + i];
+    }
+    const R gl = GL[i], gr = GR[i];
+    conservative_of<R, NV>(left, gl, ul);
+    conservative_of<R, NV>(right, gr, ur);
+    R vl = left[1], vr = right[1];
+#pragma unroll
+    for (int v = 1; v < NV - 1; ++v)
+      if (v == dir + 1) {
+        vl = left[v];
+        vr = right[v];
+      }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      fl[v] = ul[v] * vl;
+      fr[v] = ur[v] * vr;
+    }
+#pragma unroll
+    for (int v = 1; v < NV - 1; ++v)
+      if (v == dir + 1) {
+        fl[v] = fl[v] + left[NV - 1];
+        fr[v] = fr[v] + right[NV - 1];
+      }
+    fl[NV - 1] = fl[NV - 1] + vl * left[NV - 1];
+    fr[NV - 1] = fr[NV - 1] + vr * right[NV - 1];
+    const R speed = np_max(fabs(vl) + sqrt((gl * left[NV - 1]) / left[0]),
+                           fabs(vr) + sqrt((gr * right[NV - 1]) / right[0]));
+#pragma unroll
+    for (int v = 0; v < NV; ++v) out[v * n + i] = R(0.5) * ((fl[v] + fr[v]) - speed * (ur[v] - ul[v]));
+  }
+}
+
+// -- 9. block partials -> totals, in block order -------------------------------
 namespace {
 __global__ void metric_reduce_kernel(const double* part, int nblocks, int nv, double* out) {
   const int v = threadIdx.x;

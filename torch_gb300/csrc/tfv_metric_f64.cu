@@ -2,6 +2,7 @@
 // the reference's rounding).
 #define TFV_METRIC_R double
 #define TFV_METRIC_LAUNCH metric_launch_f64
+#define TFV_RUSANOV_LAUNCH rusanov_launch_f64
 #include "tfv_metric_inst.inc"
 
 namespace tfv {

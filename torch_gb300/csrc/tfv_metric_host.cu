@@ -572,6 +572,26 @@ int tfv_metric_set_current(tfv_metric* m, int32_t slot) {
   return TFV_OK;
 }
 
+int tfv_rusanov_flux(int32_t precision, int32_t nv, int64_t n, int32_t direction,
+                     const void* left, const void* right, const void* gl, const void* gr,
+                     void* out, void* stream) {
+  if (nv < 3 || nv > 5 || n < 0 || !left || !right || !gl || !gr || !out)
+    return host_fail(TFV_EINVAL, "Rusanov requires matching (3..5, m) face states");
+  if (direction < 0 || direction > nv - 3) return host_fail(TFV_EINVAL, "Invalid normal direction");
+  if (precision != TFV_FP64 && precision != TFV_FP32)
+    return host_fail(TFV_EINVAL, "precision must be fp64 or fp32");
+  if (n == 0) return TFV_OK;
+  int dev = 0, sms = 132;
+  TFV_MCUDA(cudaGetDevice(&dev));
+  TFV_MCUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sms * 8));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  TFV_MCUDA(precision == TFV_FP64
+                ? rusanov_launch_f64(nv, n, direction, left, right, gl, gr, out, grid, s)
+                : rusanov_launch_f32(nv, n, direction, left, right, gl, gr, out, grid, s));
+  return TFV_OK;
+}
+
 int tfv_metric_destroy(tfv_metric* m) {
   delete m;
   return TFV_OK;

@@ -22,6 +22,13 @@ cudaError_t metric_launch_f64(int op, int dim, const MArgs<double>& A, int arg, 
                               cudaStream_t s);
 cudaError_t metric_launch_f32(int op, int dim, const MArgs<float>& A, int arg, int grid,
                               cudaStream_t s);
+// Rusanov fluxes of n faces (rows [nv][n], primitive face states)
+cudaError_t rusanov_launch_f64(int nv, int64_t n, int dir, const void* l, const void* r,
+                               const void* gl, const void* gr, void* out, int grid,
+                               cudaStream_t s);
+cudaError_t rusanov_launch_f32(int nv, int64_t n, int dir, const void* l, const void* r,
+                               const void* gl, const void* gr, void* out, int grid,
+                               cudaStream_t s);
 // out[v] = sum over blocks b < nblocks of part[b * 8 + v], v < nv, in block order
 cudaError_t metric_reduce(const double* part, int nblocks, int nv, double* out, cudaStream_t s);
 

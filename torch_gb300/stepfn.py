@@ -89,6 +89,50 @@ def hllc_flux_grid(left, right, gamma, gamma_right=None, *, direction=0, batch_s
     return out
 
 
+def rusanov_flux(left, right, gl, gr, direction, precision="fp64"):
+    """Normal Rusanov flux from primitive face states (rho, velocities, p)
+    with every tangential momentum (python/cfdSolver/torchFlux.py:80-99).
+    ``left``/``right``: (dim+2, ...) arrays; ``gl``/``gr``: gamma per face
+    (scalars broadcast)."""
+    host = isinstance(left, np.ndarray)
+    if tuple(left.shape) != tuple(right.shape) or left.ndim < 1 or left.shape[0] not in (3, 4, 5):
+        raise ValueError("Rusanov requires matching (dim+2, ...) face states")
+    if direction not in range(left.shape[0] - 2):
+        raise ValueError("Invalid normal direction")
+    dtype = torch.float64 if precision == "fp64" else torch.float32
+    dev = left.device if isinstance(left, torch.Tensor) else _device()
+    nv = left.shape[0]
+    shape = tuple(left.shape)
+    lt = _as_device(left, dtype, dev).reshape(nv, -1).contiguous()
+    rt = _as_device(right, dtype, dev).reshape(nv, -1).contiguous()
+    m = lt.shape[1]
+
+    def per_face(g):
+        if isinstance(g, torch.Tensor):
+            return g.to(device=dev, dtype=dtype).expand(shape[1:]).reshape(-1).contiguous()
+        return torch.as_tensor(np.broadcast_to(np.asarray(g, dtype=float), shape[1:]).reshape(-1)
+                               .copy(), dtype=dtype, device=dev)
+
+    g_l, g_r = per_face(gl), per_face(gr)
+    out = torch.empty_like(lt)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev)
+    _lib.check(lib.tfv_rusanov_flux(_lib.TFV_FP64 if dtype == torch.float64 else _lib.TFV_FP32,
+                                    nv, m, int(direction), _lib.ptr(lt), _lib.ptr(rt),
+                                    _lib.ptr(g_l), _lib.ptr(g_r), _lib.ptr(out),
+                                    _lib.stream_ptr(stream)))
+    stream.synchronize()
+    out = out.reshape(shape)
+    return _out(out.to(torch.float64) if host else out, host)
+
+
+def rusanov_flux_grid(left, right, gl, gr, direction, execution=None, precision="fp64"):
+    """rusanov_flux over a grid of faces in one launch
+    (python/cfdSolver/torchFlux.py:102-122: the reference batches 8,192 faces
+    per CPU task; ``execution`` is accepted and unused)."""
+    return rusanov_flux(left, right, gl, gr, direction, precision=precision)
+
+
 def _step(dim, state, spacing, dt, gamma, limiter, bcs, return_fluxes, inlet_primitive,
           precision):
     host = isinstance(state, np.ndarray)
