@@ -235,6 +235,79 @@ def reactive_leg(n=192, steps=20, warmup=3):
     return out
 
 
+def shell_3d(nr, nt, nphi):
+    """3D spherical wedge r in [0.5, 1.5], theta in [0.5, pi - 0.5], phi in
+    [0, 1]: gas at rest, pressure 4 inside r < 0.8 and 1 outside, density
+    1 with a 5% theta ripple."""
+    r = 0.5 + (np.arange(nr) + 0.5) / nr
+    th = 0.5 + (np.arange(nt) + 0.5) * (np.pi - 1.0) / nt
+    _, T, Rr = np.meshgrid(np.arange(nphi), th, r, indexing="ij")
+    p = np.zeros((5, nphi, nt, nr))
+    p[0] = 1.0 + 0.05 * np.cos(4 * T)
+    p[4] = np.where(Rr < 0.8, 4.0, 1.0)
+    return p
+
+
+def metric_leg(n=(128, 96, 96), steps=10, warmup=2, cpu_n=(96, 64, 64), cpu_steps=3):
+    """Metric / face-boundary step (MUSCL-Rusanov-SSPRK2) on a 3D spherical
+    wedge, radial outflow and pressure outlet, walls in theta and phi,
+    Superbee: FP32 and FP64 on the GPU against the oracle on the host."""
+    import torch
+
+    import torch_gb300
+    from oracle import metric as oracle_metric
+
+    lengths = [1.0, np.pi - 1.0, 1.0]
+    kw = dict(t_end=1e9, cfl=0.4, limiter="Superbee", geometry="spherical",
+              origins=[0.5, 0.5, 0.0], max_steps=10 ** 9,
+              face_boundaries={"x_min": "wall", "x_max": {"type": "pressure_outlet",
+                                                          "pressure": 1.0,
+                                                          "backflow": [1.0, -0.1, 0.0, 0.0,
+                                                                       1.0]},
+                               "y_min": "wall", "y_max": "wall", "z_min": "wall",
+                               "z_max": "wall"})
+    cells = n[0] * n[1] * n[2]
+    out = {"workload": f"3D spherical wedge {n[0]}x{n[1]}x{n[2]}, r in [0.5,1.5], pressure "
+                       "outlet at r = 1.5, walls elsewhere, Superbee, CFL 0.4; "
+                       f"{steps} steps after {warmup}"}
+    prim = shell_3d(*n)
+    for prec in ("fp32", "fp64"):
+        sim = torch_gb300.Simulation(prim, lengths, precision=prec, **kw)
+        sim.advance(warmup)
+        t0 = time.perf_counter()
+        sim.advance(steps)  # synchronous: each step waits for its dt and stage checks
+        ms = (time.perf_counter() - t0) * 1e3 / steps
+        bpc = 40 if prec == "fp32" else 80
+        out[prec] = {"value": cells / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+                     "fallback_steps": sim.fallback_steps,
+                     "hbm_gbs_at_algorithmic_bytes": bpc * cells / (ms * 1e-3) / 1e9,
+                     "bytes_per_cell": bpc}
+        del sim
+        torch.cuda.empty_cache()
+    out["fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    # the oracle (NumPy, the reference's algorithm) on a bounded sample
+    small = shell_3d(*cpu_n)
+    c = dict(dimension=3, counts_xyz=list(cpu_n), lengths_xyz=lengths,
+             boundaries_xyz=["Open"] * 3, geometry="spherical", origins_xyz=[0.5, 0.5, 0.0],
+             inlet_primitive=[1.0, 0.0, 100.0, 101325.0])
+    from torch_gb300 import metric as host_metric
+    faces = host_metric.normalize_faces(c, kw["face_boundaries"])
+    ref = oracle_metric.OracleMetricSimulation(small, lengths, t_end=1e9, cfl=0.4,
+                                               limiter="Superbee", geometry="spherical",
+                                               origins=[0.5, 0.5, 0.0], faces=faces)
+    if cpu_steps == 0:
+        return out
+    t0 = time.perf_counter()
+    for _ in range(cpu_steps):
+        ref.step()
+    cpu_s = time.perf_counter() - t0
+    cpu_cells = cpu_n[0] * cpu_n[1] * cpu_n[2]
+    out["cpu_baseline"] = {"value": cpu_cells * cpu_steps / cpu_s, "unit": UNIT, "cores": 1,
+                           "kind": "port", "sample": f"oracle, {cpu_n[0]}x{cpu_n[1]}x{cpu_n[2]} "
+                                                     f"wedge, {cpu_steps} steps"}
+    return out
+
+
 def batched_leg(steps=500, count=64, seed=4, fp64_steps=20):
     """64 quadrant grids (N from {64..1024}), MINBEE, FP32, `steps` steps each
     in one batch (autotuned tile, graph-captured), against the same grids
@@ -359,6 +432,11 @@ def main():
     ap.add_argument("--tile", default=None, help="tx,ty,chunk[,persistent_ctas] of the FP32 step")
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-reactive", action="store_true")
+    ap.add_argument("--skip-metric", action="store_true")
+    ap.add_argument("--metric-cells", default="128,96,96",
+                    help="cells (r, theta, phi) of the metric / face-boundary leg's wedge")
+    ap.add_argument("--metric-only", action="store_true",
+                    help="run only the metric / face-boundary leg (--steps, --warmup) and print it")
     ap.add_argument("--skip-served", action="store_true")
     ap.add_argument("--served-count", type=int, default=16)
     ap.add_argument("--e2e-sessions", type=int, default=4,
@@ -376,6 +454,12 @@ def main():
 
     local = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(local)
+    if args.metric_only:
+        leg = metric_leg(n=tuple(int(v) for v in args.metric_cells.split(",")),
+                         steps=args.steps, warmup=args.warmup,
+                         cpu_steps=0 if args.skip_cpu else 3)
+        print(json.dumps({"metric_leg": leg}), flush=True)
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -512,6 +596,8 @@ def main():
 
     if rank == 0 and not args.skip_reactive:
         extra["reactive"] = reactive_leg()
+    if rank == 0 and not args.skip_metric:
+        extra["metric"] = metric_leg(n=tuple(int(v) for v in args.metric_cells.split(",")))
     if rank == 0 and not args.skip_batched:
         extra["batched"] = batched_leg()
     if rank == 0 and not args.skip_served:

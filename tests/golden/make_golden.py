@@ -540,6 +540,86 @@ def rusanov_cases(R):
     np.savez_compressed(OUT / "rusanov.npz", **out)
 
 
+def output_cases(R):
+    """The reference's field output (torchIO.py:122-733): VTK rectilinear and
+    structured snapshots, XDMF snapshots with their HDF5 heavy data, and the
+    temporal series (frames, .pvd, .xdmf, manifest) of short runs.  Every
+    file is recorded as bytes (HDF5 files as their datasets), with the session
+    attributes at each frame, so the GPU session's writers can be compared
+    byte for byte."""
+    import tempfile
+    sys.modules["h5py"] = _RecordingHDF5("h5py")
+    io = importlib.import_module("cfdSolver.torchIO")
+    S = R.torchSession.Simulation
+    out = {}
+
+    def snap(key, s):
+        out[f"{key}|state"] = s.state.copy()
+        for name in ("lam", "beta"):
+            if getattr(s, name) is not None:
+                out[f"{key}|{name}"] = getattr(s, name).copy()
+        out[f"{key}|scalars"] = np.array([s.time, s.steps])
+        out[f"{key}|integrals"] = np.stack((s.initial_integral, s.boundary_integral,
+                                            s.source_integral))
+        out[f"{key}|config"] = np.frombuffer(json.dumps(s.config).encode(), dtype=np.uint8)
+        out[f"{key}|run_id"] = np.frombuffer(s.run_id.encode(), dtype=np.uint8)
+
+    def files(key, folder):
+        for f in sorted(Path(folder).iterdir()):
+            if f.suffix == ".h5":
+                with _RecordingHDF5.File(f) as h:
+                    for name, value in h.data.items():
+                        out[f"{key}|file/{f.name}/{name}"] = value
+            else:
+                out[f"{key}|file/{f.name}"] = np.frombuffer(f.read_bytes(), dtype=np.uint8)
+
+    rng = np.random.default_rng(5)
+    p2 = np.ones((4, 4, 6))
+    p2[0] += 0.3 * rng.random((4, 6))
+    p2[1:3] = 0.1 * rng.standard_normal((2, 4, 6))
+    p2[3] += rng.random((4, 6))
+    cases = {
+        "vtr2d": S(p2, [1.0, 0.8], t_end=0.05, limiter="MINBEE"),
+        "vts2d_znd": S(np.stack((p2[0], p2[1], p2[2], 1e5 * p2[3])), [1.0, 1.0],
+                       geometry="spherical", origins=[0.5, 0.5], t_end=2e-5, reactive=True,
+                       kinetic_model="znd"),
+    }
+    p1 = np.ones((3, 7))
+    p1[0] += np.linspace(0, 0.5, 7)
+    cases["vtr1d"] = S(p1, [1.0], t_end=0.05)
+    p3 = np.ones((5, 3, 4, 5))
+    p3[1] = 0.2
+    cases["vts3d_annular"] = S(p3, [1.0, 1.0, 0.5], geometry="annular",
+                               origins=[0.5, 0.0, 0.0], t_end=0.05)
+    with tempfile.TemporaryDirectory() as tmp:
+        for key, s in cases.items():
+            folder = Path(tmp) / key
+            folder.mkdir()
+            recorded = []
+            original = io.TemporalWriter.append
+
+            def append(self, session, _orig=original, _rec=recorded):
+                _rec.append(len(_rec))
+                snap(f"{key}/frame{len(_rec) - 1}", session)
+                return _orig(self, session)
+
+            io.TemporalWriter.append = append
+            try:
+                s.run(step_limit=3, output_prefix=folder / "series", output_every=2,
+                      formats=("vtk",) if key.startswith("vts2d") else ("vtk", "xdmf"))
+            finally:
+                io.TemporalWriter.append = original
+            out[f"{key}|frames"] = np.array([len(recorded)])
+            single = Path(tmp) / (key + "_single")
+            single.mkdir()
+            snap(f"{key}/single", s)
+            io.write_vtk(single / ("snap" + (".vts" if "vts" in key else ".vtr")), s)
+            io.write_xdmf(single / "snap.xdmf", s)
+            files(f"{key}/series", folder)
+            files(f"{key}/single", single)
+    np.savez_compressed(OUT / "output.npz", **out)
+
+
 def large_cfl_case(R):
     """2D explosion at CFL 0.8 (rejected by Simulation): dt from the session
     formula, step function called directly, 12 steps on a 40x40 grid."""
@@ -607,6 +687,9 @@ def main():
     if sys.argv[1:] == ["rusanov"]:  # regenerate rusanov.npz alone
         rusanov_cases(R)
         return
+    if sys.argv[1:] == ["output"]:  # regenerate output.npz alone
+        output_cases(R)
+        return
     rng = np.random.default_rng(20261203)
     hllc_cases(R, rng)
     step3d_cases(R, rng)
@@ -618,6 +701,7 @@ def main():
     checkpoint_cases(R)
     metric_cases(R)
     rusanov_cases(R)
+    output_cases(R)
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -27,10 +27,22 @@ SOLVER_VERSION = "1.4"
 READABLE_VERSIONS = ((1, "1.1"), (2, "1.2"), (2, "1.4"))
 
 
+def coordinates(config):
+    """Names of the logical coordinates (torchGeometry.py:12-27)."""
+    dim = config["dimension"]
+    g = config.get("geometry", "cartesian")
+    if g == "cartesian":
+        return list("xyz"[:dim])
+    if g == "spherical":
+        return ["r", "theta", "phi"][:dim]
+    if g == "cylindrical" and dim == 2:
+        return ["r", "z"]
+    return ["r", "theta", "z"][:dim]
+
+
 def component_names(config):
-    """Dataset names of the conservative components (torchGeometry.py:12-31,
-    Cartesian coordinates)."""
-    return ["rho"] + ["momentum_" + a for a in "xyz"[:config["dimension"]]] + ["energy"]
+    """Dataset names of the conservative components (torchGeometry.py:30-31)."""
+    return ["rho"] + ["momentum_" + a for a in coordinates(config)] + ["energy"]
 
 
 def physical_state(state):
@@ -90,9 +102,11 @@ def metadata(session):
                 source_integral=integrals[2], current_integral=np.asarray(session.integral))
 
 
-def contents(session):
+def contents(session, visualization=False):
     """{dataset name: array} of a checkpoint: ``metadata`` as uint8 bytes and
-    the flat little-endian float64 state datasets (torchIO.py:192-218)."""
+    the flat little-endian float64 state datasets; with ``visualization``
+    also the mesh points and cells and the derived fields that an XDMF file
+    points at (torchIO.py:192-218)."""
     out = {"metadata": np.frombuffer(encode(metadata(session)), dtype=np.uint8)}
     state = np.asarray(session.state)
     for name, row in zip(component_names(session.config), state):
@@ -100,7 +114,31 @@ def contents(session):
     for name, value in (("lambda", session.lam), ("beta", session.beta)):
         if value is not None:
             out["state/" + name] = np.asarray(value).ravel().astype("<f8")
+    if visualization:
+        from . import output
+        _, points, cells = output.mesh(session)
+        out["mesh/points"] = points.astype("<f8")
+        out["mesh/cells"] = cells
+        for name, value in output.fields(session).items():
+            out["fields/" + name] = value.astype("<f8")
     return out
+
+
+def atomic(path, write):
+    """Replace `path` atomically: write a temporary file in the same
+    directory, fsync it and rename it over the target (torchIO.py:49-63)."""
+    path = Path(path)
+    path.parent.mkdir(parents=True, exist_ok=True)
+    fd, temp = tempfile.mkstemp(prefix="." + path.name + ".", suffix=".tmp", dir=path.parent)
+    os.close(fd)
+    try:
+        write(Path(temp))
+        with open(temp, "rb") as handle:
+            os.fsync(handle.fileno())
+        os.replace(temp, path)
+    finally:
+        if os.path.exists(temp):
+            os.unlink(temp)
 
 
 class Snapshot:
@@ -216,30 +254,23 @@ def _h5py():
     return h5py
 
 
-def write(path, session):
+def write(path, session, visualization=False):
     """Write a checkpoint atomically (temporary file in the same directory,
     fsync, rename), with Fletcher-32 checksums on the state datasets
     (torchIO.py:49-63, 192-230).  Returns the path as a string."""
-    data = contents(session)  # validate before touching the file system
+    data = contents(session, visualization)  # validate before touching the file system
     h5py = _h5py()
-    path = Path(path)
-    path.parent.mkdir(parents=True, exist_ok=True)
-    fd, temp = tempfile.mkstemp(prefix="." + path.name + ".", suffix=".tmp", dir=path.parent)
-    os.close(fd)
-    try:
+
+    def dump(temp):
         with h5py.File(temp, "w") as handle:
             for name, value in data.items():
-                if name == "metadata":
-                    handle.create_dataset(name, data=value)
-                else:
+                if name.startswith("state/"):
                     handle.create_dataset(name, data=value, fletcher32=True)
+                else:
+                    handle.create_dataset(name, data=value)
             handle.flush()
-        with open(temp, "rb") as handle:
-            os.fsync(handle.fileno())
-        os.replace(temp, path)
-    finally:
-        if os.path.exists(temp):
-            os.unlink(temp)
+
+    atomic(path, dump)
     return str(path)
 
 

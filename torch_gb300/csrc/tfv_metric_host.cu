@@ -163,6 +163,10 @@ struct Driver {
   double* res;        // device [kSlots][8]
   double* part;
   cudaStream_t s;
+  // state whose primitives, gamma and source are in P, G, K (and whose
+  // source sum is in res[prim_slot]); a right-hand side of that state reuses them
+  const void* prim_state = nullptr;
+  int prim_slot = -1;
 
   cudaError_t launch(int op, int arg, int grid) {
     return sizeof(R) == 8
@@ -183,13 +187,22 @@ struct Driver {
     set_input(v);
     const int g = reduce_grid(m->nc);
     TFV_MCUDA(launch(kMOpPrim, 0, g));
+    prim_state = v.u;
+    prim_slot = slot;
     return reduce(slot, g);
   }
   // one SSPRK2 right-hand side: K, KQ, the source and outward sums
   int rhs(const View& v, bool first_order, int slot_source, int slot_outward) {
     A.first_order = first_order ? 1 : 0;
-    int r = prim(v, slot_source);
-    if (r) return r;
+    if (prim_state == v.u && prim_slot >= 0) {  // primitives of v already computed (dt pass)
+      set_input(v);
+      if (prim_slot != slot_source)
+        TFV_MCUDA(cudaMemcpyAsync(res + slot_source * 8, res + prim_slot * 8, 8 * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, s));
+    } else {
+      int r = prim(v, slot_source);
+      if (r) return r;
+    }
     for (int d = 0; d < m->dim; ++d) TFV_MCUDA(launch(kMOpFace, d, grid_for(m, m->nf[d])));
     int64_t plane = 0;
     for (int d = 0; d < m->dim; ++d) plane = std::max<int64_t>(plane, m->nc / m->cfg.n[d]);

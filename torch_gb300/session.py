@@ -488,10 +488,13 @@ class Simulation:
             output_every=1, formats=("vtk", "xdmf"), chunk=64):
         """Advance to t_end or by `step_limit` steps (torchSession.py:578-632).
         With `checkpoint`, a checkpoint is written whenever the step count
-        reaches a multiple of `checkpoint_every` and once at the end; steps
-        are enqueued in chunks that stop at those multiples, so no numerical
-        step is shortened.  Field output (VTK/XDMF) is the reference's host IO
-        and is not produced here."""
+        reaches a multiple of `checkpoint_every` and once at the end; with
+        `output_prefix`, a VTK / XDMF frame at the start, at every multiple of
+        `output_every` and at the end (torch_gb300/output.py: the state is
+        copied to pinned host memory on the session's stream and a host thread
+        writes the files while the GPU keeps stepping).  Steps are enqueued in
+        chunks that stop at those multiples, so no numerical step is
+        shortened."""
         for value in (step_limit, checkpoint_every, output_every):
             if value is not None and (not isinstance(value, int) or value < 0):
                 raise ValueError("Step intervals must be nonnegative integers")
@@ -499,25 +502,37 @@ class Simulation:
             raise ValueError("checkpoint_every requires a checkpoint destination")
         if output_prefix and output_every < 1:
             raise ValueError("output_every must be positive")
-        if output_prefix:
-            raise NotImplementedError("VTK/XDMF field output is written by the reference's torchIO")
-        remaining = step_limit
-        while not self.completed and (remaining is None or remaining > 0):
-            self._raise_pending()
-            k = chunk if remaining is None else min(chunk, remaining)
-            if checkpoint and checkpoint_every:
-                k = min(k, checkpoint_every - self.steps % checkpoint_every)
-            before = self.steps
-            self._engine.advance(k)
-            self._engine.refresh()
-            if remaining is not None:
-                remaining -= self.steps - before
-            self._raise_pending()
-            if (checkpoint and checkpoint_every and self.steps != before
-                    and self.steps % checkpoint_every == 0):
+        writer = None
+        if output_prefix:  # frames are copied off the GPU and written by a host thread
+            from .output import AsyncWriter
+            writer = AsyncWriter(output_prefix, self, formats)
+        try:
+            remaining = step_limit
+            while not self.completed and (remaining is None or remaining > 0):
+                self._raise_pending()
+                k = chunk if remaining is None else min(chunk, remaining)
+                if checkpoint and checkpoint_every:
+                    k = min(k, checkpoint_every - self.steps % checkpoint_every)
+                if writer:
+                    k = min(k, output_every - self.steps % output_every)
+                before = self.steps
+                self._engine.advance(k)
+                self._engine.refresh()
+                if remaining is not None:
+                    remaining -= self.steps - before
+                self._raise_pending()
+                if (checkpoint and checkpoint_every and self.steps != before
+                        and self.steps % checkpoint_every == 0):
+                    self.save(checkpoint)
+                if writer and self.steps != before and self.steps % output_every == 0:
+                    writer.append(self)
+            if checkpoint:
                 self.save(checkpoint)
-        if checkpoint:
-            self.save(checkpoint)
+            if writer:
+                writer.append(self)
+        finally:
+            if writer:
+                writer.close()
         return self
 
     # -- checkpoint interchange (torchSession.py:634-651) ----------------------
