@@ -2,7 +2,7 @@
 the GPU asynchronously and writes the same series the reference wrote for
 the same runs (tests/golden/output.npz): VTK files, collections and the
 manifest byte for byte, HDF5 datasets value for value, the metadata's
-current integral (a GPU sum) at 1e-12."""
+integrals (GPU sums, in another order than NumPy's) at 1e-12."""
 
 import json
 from pathlib import Path
@@ -54,8 +54,9 @@ def test_gpu_series_matches_reference(case, fake_h5py, tmp_path):
                 got = z[dataset.replace("/", "|")]
             if dataset == "metadata":
                 mine, ref = json.loads(bytes(got).decode()), json.loads(bytes(value).decode())
-                np.testing.assert_allclose(mine.pop("current_integral"),
-                                           ref.pop("current_integral"), rtol=1e-12, atol=1e-15)
+                for key in ("current_integral", "boundary_integral", "source_integral"):
+                    np.testing.assert_allclose(mine.pop(key), ref.pop(key), rtol=1e-12,
+                                               atol=1e-15)  # GPU sums: another order
                 assert mine == ref
             else:
                 np.testing.assert_array_equal(got, value, err_msg=name)
