@@ -107,7 +107,7 @@ template <typename R, int NV>
 __device__ __forceinline__ void load_cell(const MArgs<R>& A, int64_t off, MCell<R, NV>& c) {
 #pragma unroll
   for (int v = 0; v < NV; ++v) c.p[v] = A.P[v * A.nc + off];
-  c.g = A.reactive ? A.G[off] : R(A.gamma);
+  c.g = A.reactive ? A.G[off] : A.gam;
   c.q[0] = A.nfrac > 0 ? A.Q[0][off] : R(0);
   c.q[1] = A.nfrac > 1 ? A.Q[1][off] : R(0);
 }
@@ -115,7 +115,7 @@ __device__ __forceinline__ void load_cell(const MArgs<R>& A, int64_t off, MCell<
 // Boundary state built from the boundary cell (torchBoundaries.py:185-246).
 // side -1 low face, +1 high face; d the direction.  Returns error bits.
 template <typename R, int NV>
-__device__ __forceinline__ int ghost_state(const MArgs<R>& A, const MFace& F, int d, int side,
+__device__ __forceinline__ int ghost_state(const MArgs<R>& A, const MFace<R>& F, int d, int side,
                                            MCell<R, NV>& c) {
   const int n = d + 1;
   const R gamma = c.g;  // the boundary cell's gamma
@@ -124,18 +124,18 @@ __device__ __forceinline__ int ghost_state(const MArgs<R>& A, const MFace& F, in
     return 0;
   }
   if (F.type == kFaceInflow || F.type == kFaceStagnation) {
-    const R g = A.reactive ? gamma_of_lambda(R(F.lam)) : gamma;
+    const R g = A.reactive ? F.gam : gamma;
     c.g = g;
-    c.q[0] = R(F.lam);
-    c.q[1] = R(F.beta);
+    c.q[0] = F.lam;
+    c.q[1] = F.beta;
     if (F.type == kFaceInflow) {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) c.p[v] = R(F.prim[v]);
+      for (int v = 0; v < NV; ++v) c.p[v] = F.prim[v];
       return 0;
     }
     const R sound = sqrt((gamma * c.p[NV - 1]) / c.p[0]);
     const R riemann = R(-side) * c.p[n] - (R(2) * sound) / (gamma - R(1));
-    const R a0sq = (g * R(F.rgas)) * R(F.t0);
+    const R a0sq = (g * F.rgas) * F.t0;
     const R k = (g + R(1)) / (g - R(1));
     const R disc = riemann * riemann - k * ((R(0.5) * (g - R(1))) * (riemann * riemann) - a0sq);
     if (disc < R(0)) return kMErrReservoirSolution;
@@ -149,7 +149,7 @@ __device__ __forceinline__ int ghost_state(const MArgs<R>& A, const MFace& F, in
 #pragma unroll
     for (int v = 1; v < NV - 1; ++v) c.p[v] = R(0);
     c.p[n] = R(-side) * speed;
-    c.p[NV - 1] = R(F.p0) * tpow((a * a) / a0sq, g / (g - R(1)));
+    c.p[NV - 1] = F.p0 * tpow((a * a) / a0sq, g / (g - R(1)));
     c.p[0] = (g * c.p[NV - 1]) / (a * a);
     return 0;
   }
@@ -158,7 +158,7 @@ __device__ __forceinline__ int ghost_state(const MArgs<R>& A, const MFace& F, in
     const R a = sqrt((g * c.p[NV - 1]) / c.p[0]);
     const R un = R(side) * c.p[n];
     const bool subsonic = un < a;
-    const R pr = R(F.pressure);
+    const R pr = F.pressure;
     const R rho = c.p[0] * tpow(pr / c.p[NV - 1], R(1) / g);
     const R anew = sqrt((g * pr) / rho);
     const R velocity = un + (R(2) * (a - anew)) / (g - R(1));
@@ -171,10 +171,10 @@ __device__ __forceinline__ int ghost_state(const MArgs<R>& A, const MFace& F, in
     }
     if (back) {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) c.p[v] = R(F.prim[v]);
-      if (A.reactive) c.g = gamma_of_lambda(R(F.lam));
-      c.q[0] = R(F.lam);
-      c.q[1] = R(F.beta);
+      for (int v = 0; v < NV; ++v) c.p[v] = F.prim[v];
+      if (A.reactive) c.g = F.gam;
+      c.q[0] = F.lam;
+      c.q[1] = F.beta;
     }
     return 0;
   }
@@ -250,14 +250,20 @@ __global__ void __launch_bounds__(kMThreads) metric_prim_kernel(MArgs<R> A) {
   constexpr int NV = DIM + 2;
   __shared__ double red[32];
   double part[NV];
+  // single precision: this thread's source sums with compensation (Kahan),
+  // converted once; block and grid sums are double
+  R ksum[NV], kcomp[NV];
 #pragma unroll
-  for (int v = 0; v < NV; ++v) part[v] = 0.0;
+  for (int v = 0; v < NV; ++v) {
+    part[v] = 0.0;
+    ksum[v] = kcomp[v] = R(0);
+  }
   for (int64_t off = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; off < A.nc;
        off += (int64_t)gridDim.x * blockDim.x) {
     R u[NV], p[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) u[v] = A.U[v * A.nc + off];
-    const R g = A.reactive ? gamma_of_lambda(A.Q[0][off]) : R(A.gamma);
+    const R g = A.reactive ? gamma_of_lambda(A.Q[0][off]) : A.gam;
     primitive_of<R, NV>(u, g, p);
 #pragma unroll
     for (int v = 0; v < NV; ++v) A.P[v * A.nc + off] = p[v];
@@ -290,10 +296,23 @@ __global__ void __launch_bounds__(kMThreads) metric_prim_kernel(MArgs<R> A) {
         s[2] = (((-rho) * p[1]) * p[2]) * radial;
       }
 #pragma unroll
-      for (int v = 0; v < NV; ++v) part[v] += (double)(s[v] * vol);
+      for (int v = 0; v < NV; ++v) {
+        if constexpr (Exact<R>::value) {
+          part[v] += s[v] * vol;
+        } else {
+          const R y = s[v] * vol - kcomp[v];
+          const R t = ksum[v] + y;
+          kcomp[v] = (t - ksum[v]) - y;
+          ksum[v] = t;
+        }
+      }
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) A.K[v * A.nc + off] = s[v];
+  }
+  if constexpr (!Exact<R>::value) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) part[v] = (double)ksum[v] - (double)kcomp[v];
   }
 #pragma unroll
   for (int v = 0; v < NV; ++v) {

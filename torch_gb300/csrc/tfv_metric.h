@@ -37,13 +37,17 @@ enum : int32_t {
   kMErrFinal = 128,            // state after the closing reaction half not physical
 };
 
+// One face boundary in the kernels' arithmetic type (converted once on the
+// host, so single-precision kernels do no double-precision conversions).
+template <typename R>
 struct MFace {
   int32_t type;
   int32_t has_backflow;
-  double prim[5];   // inflow primitive state, or the pressure outlet's backflow state
-  double lam, beta; // fractions carried in by inflow / backflow / reservoir
-  double pressure;  // pressure outlet
-  double p0, t0, rgas;  // stagnation inlet: total pressure, temperature, gas constant
+  R prim[5];   // inflow primitive state, or the pressure outlet's backflow state
+  R lam, beta; // fractions carried in by inflow / backflow / reservoir
+  R gam;       // gamma(lam) of the carried-in gas (reactive sessions)
+  R pressure;  // pressure outlet
+  R p0, t0, rgas;  // stagnation inlet: total pressure, temperature, gas constant
 };
 
 constexpr int kMReduceBlocks = 512;  // fixed block count of every reduction (deterministic)
@@ -60,9 +64,10 @@ struct MArgs {
   int32_t first_order;
   int32_t znd;
   double gamma;
+  R gam;              // gamma in the arithmetic type
   double dt;          // stage time step
   int32_t periodic[3];  // face pair of each direction is periodic
-  const MFace* face;  // [6] in device memory (x_min, x_max, y_min, ...)
+  const MFace<R>* face;  // [6] in device memory (x_min, x_max, y_min, ...)
   InstDesc chem;      // chemistry constants (q, ea, a, closure) for react_cell
   const R* vf[3];     // volume factors per axis
   const R* ff[3][3];  // face-area factors [direction][axis]

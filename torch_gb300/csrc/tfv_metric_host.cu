@@ -110,7 +110,8 @@ MArgs<R> make_args(const tfv_metric* m) {
   A.gamma = m->cfg.gamma;
   for (int d = 0; d < 3; ++d)
     A.periodic[d] = d < m->dim && m->cfg.faces[2 * d].type == TFV_FACE_PERIODIC;
-  A.face = reinterpret_cast<const MFace*>(m->ws + m->off_faces);
+  A.gam = (R)m->cfg.gamma;
+  A.face = reinterpret_cast<const MFace<R>*>(m->ws + m->off_faces);
   A.chem.q = m->cfg.q;
   A.chem.ea = m->cfg.ea;
   A.chem.a = m->cfg.a;
@@ -372,6 +373,30 @@ int metric_step(tfv_metric* m) {
 }
 
 template <typename R>
+int upload_faces(tfv_metric* m) {
+  MFace<R> faces[6];
+  std::memset(faces, 0, sizeof(faces));
+  for (int f = 0; f < 6; ++f) {
+    const tfv_metric_face& s = m->cfg.faces[f];
+    MFace<R>& F = faces[f];
+    F.type = f < 2 * m->dim ? s.type : kFaceOutflow;
+    F.has_backflow = s.has_backflow;
+    for (int v = 0; v < 5; ++v) F.prim[v] = (R)s.primitive[v];
+    F.lam = (R)s.lambda_;
+    F.beta = (R)s.beta;
+    F.gam = (R)((4.5 - s.lambda_) / (3.5 - s.lambda_));  // gamma_calc (torchSolver.py:71-82)
+    F.pressure = (R)s.pressure;
+    F.p0 = (R)s.total_pressure;
+    F.t0 = (R)s.total_temperature;
+    F.rgas = (R)s.gas_constant;
+  }
+  TFV_MCUDA(cudaMemcpyAsync(m->ws + m->off_faces, faces, sizeof(faces), cudaMemcpyHostToDevice,
+                            m->stream));
+  TFV_MCUDA(cudaStreamSynchronize(m->stream));
+  return TFV_OK;
+}
+
+template <typename R>
 int metric_integrals(tfv_metric* m, double* out) {
   Driver<R> D;
   D.m = m;
@@ -450,7 +475,7 @@ int tfv_metric_create(int32_t precision, const tfv_metric_config* cfg, const dou
     m->off_w[d] = take(m->esz * m->nv * m->nf[d]);
     m->off_t[d] = take(m->esz * 2 * m->nf[d]);
   }
-  m->off_faces = take(sizeof(MFace) * 6);
+  m->off_faces = take(sizeof(MFace<double>) * 6);
   m->off_fac = take(m->esz * m->factors.size());
   m->off_part = take(sizeof(double) * kMReduceBlocks * 8);
   m->off_res = take(sizeof(double) * kSlots * 8);
@@ -487,24 +512,9 @@ int tfv_metric_bind(tfv_metric* m, void* workspace, void* const* states, void* c
   int dev = 0;
   TFV_MCUDA(cudaGetDevice(&dev));
   TFV_MCUDA(cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, dev));
-  // face table and factors in the workspace (factors in the arithmetic type)
-  MFace faces[6];
-  std::memset(faces, 0, sizeof(faces));
-  for (int f = 0; f < 6; ++f) {
-    const tfv_metric_face& s = m->cfg.faces[f];
-    MFace& F = faces[f];
-    F.type = f < 2 * m->dim ? s.type : kFaceOutflow;
-    F.has_backflow = s.has_backflow;
-    for (int v = 0; v < 5; ++v) F.prim[v] = s.primitive[v];
-    F.lam = s.lambda_;
-    F.beta = s.beta;
-    F.pressure = s.pressure;
-    F.p0 = s.total_pressure;
-    F.t0 = s.total_temperature;
-    F.rgas = s.gas_constant;
-  }
-  TFV_MCUDA(cudaMemcpyAsync(m->ws + m->off_faces, faces, sizeof(faces), cudaMemcpyHostToDevice,
-                            m->stream));
+  // face table and factors in the workspace, in the arithmetic type
+  int r0 = m->precision == TFV_FP64 ? upload_faces<double>(m) : upload_faces<float>(m);
+  if (r0) return r0;
   if (m->precision == TFV_FP64) {
     TFV_MCUDA(cudaMemcpyAsync(m->ws + m->off_fac, m->factors.data(),
                               sizeof(double) * m->factors.size(), cudaMemcpyHostToDevice, m->stream));
