@@ -458,7 +458,7 @@ def main():
         leg = metric_leg(n=tuple(int(v) for v in args.metric_cells.split(",")),
                          steps=args.steps, warmup=args.warmup,
                          cpu_steps=0 if args.skip_cpu else 3)
-        print(json.dumps({"metric_leg": leg}), flush=True)
+        print(json.dumps({"metric_kernel": leg}), flush=True)
         return
     dist = None
     if world > 1:
@@ -597,7 +597,8 @@ def main():
     if rank == 0 and not args.skip_reactive:
         extra["reactive"] = reactive_leg()
     if rank == 0 and not args.skip_metric:
-        extra["metric"] = metric_leg(n=tuple(int(v) for v in args.metric_cells.split(",")))
+        extra["metric_kernel"] = metric_leg(
+            n=tuple(int(v) for v in args.metric_cells.split(",")))
     if rank == 0 and not args.skip_batched:
         extra["batched"] = batched_leg()
     if rank == 0 and not args.skip_served:
