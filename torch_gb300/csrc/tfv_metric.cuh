@@ -322,6 +322,69 @@ __global__ void __launch_bounds__(kMThreads) metric_prim_kernel(MArgs<R> A) {
 }
 
 // -- 2. Rusanov fluxes of one direction, weighted by the face areas ------------
+// Rusanov flux of face f (padded cells f and f + 1 with their slopes),
+// weighted by the face area, and the upwind fraction transport
+// (torchFiniteVolume.py:160-226).
+template <typename R, int DIM, int D>
+__device__ __forceinline__ void emit_face(const MArgs<R>& A, int f, const MIdx& c, int64_t idx,
+                                          const MCell<R, DIM + 2>& cl,
+                                          const MCell<R, DIM + 2>& cr, const R* sl, const R* sr) {
+  constexpr int NV = DIM + 2;
+  constexpr int d = D;
+  const int n = A.n[d];
+  const int64_t nf = A.nf[d];
+  R left[NV], right[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    left[v] = cl.p[v] + R(0.5) * sl[v];
+    right[v] = cr.p[v] - R(0.5) * sr[v];
+  }
+  R gl = cl.g, gr = cr.g;
+  // walls mirror the interior face state (torchFiniteVolume.py:164-181)
+  if (f == 0 && A.face[2 * d].type == kFaceWall) {  // face table in device memory
+#pragma unroll
+    for (int v = 0; v < NV; ++v) left[v] = right[v];
+    gl = gr;
+    left[d + 1] = -left[d + 1];
+  }
+  if (f == n && A.face[2 * d + 1].type == kFaceWall) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) right[v] = left[v];
+    gr = gl;
+    right[d + 1] = -right[d + 1];
+  }
+  // Rusanov (torchFiniteVolume.py:186-207)
+  R ul[NV], ur[NV], fl[NV], fr[NV];
+  conservative_of<R, NV>(left, gl, ul);
+  conservative_of<R, NV>(right, gr, ur);
+  const R vl = left[d + 1], vr = right[d + 1];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    fl[v] = ul[v] * vl;
+    fr[v] = ur[v] * vr;
+  }
+  fl[d + 1] = fl[d + 1] + left[NV - 1];
+  fr[d + 1] = fr[d + 1] + right[NV - 1];
+  fl[NV - 1] = fl[NV - 1] + vl * left[NV - 1];
+  fr[NV - 1] = fr[NV - 1] + vr * right[NV - 1];
+  const R speed = np_max(fabs(vl) + sqrt((gl * left[NV - 1]) / left[0]),
+                         fabs(vr) + sqrt((gr * right[NV - 1]) / right[0]));
+  const R ar = area<R, DIM>(A, d, f, c);
+  R* W = A.W[d];
+  R flux0 = R(0);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const R flux = ((fl[v] + fr[v]) - (ur[v] - ul[v]) * speed) * R(0.5);
+    if (v == 0) flux0 = flux;
+    W[v * nf + idx] = flux * ar;
+  }
+  // first-order upwind transport of the fractions (torchFiniteVolume.py:223-226)
+  for (int q = 0; q < A.nfrac; ++q) {
+    const R up = flux0 >= R(0) ? cl.q[q] : cr.q[q];
+    A.T[d][q * nf + idx] = (flux0 * up) * ar;
+  }
+}
+
 template <typename R, int DIM, int D>
 __global__ void __launch_bounds__(kMThreads) metric_face_kernel(MArgs<R> A) {
   constexpr int NV = DIM + 2;
@@ -386,56 +449,7 @@ __global__ void __launch_bounds__(kMThreads) metric_face_kernel(MArgs<R> A) {
         cell_slope<R, NV>(a, b, e, A.limiter, sr);
       }
     }
-    R left[NV], right[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      left[v] = cl.p[v] + R(0.5) * sl[v];
-      right[v] = cr.p[v] - R(0.5) * sr[v];
-    }
-    R gl = cl.g, gr = cr.g;
-    // walls mirror the interior face state (torchFiniteVolume.py:164-181)
-    if (f == 0 && A.face[2 * d].type == kFaceWall) {  // face table in device memory
-#pragma unroll
-      for (int v = 0; v < NV; ++v) left[v] = right[v];
-      gl = gr;
-      left[d + 1] = -left[d + 1];
-    }
-    if (f == n && A.face[2 * d + 1].type == kFaceWall) {
-#pragma unroll
-      for (int v = 0; v < NV; ++v) right[v] = left[v];
-      gr = gl;
-      right[d + 1] = -right[d + 1];
-    }
-    // Rusanov (torchFiniteVolume.py:186-207)
-    R ul[NV], ur[NV], fl[NV], fr[NV];
-    conservative_of<R, NV>(left, gl, ul);
-    conservative_of<R, NV>(right, gr, ur);
-    const R vl = left[d + 1], vr = right[d + 1];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      fl[v] = ul[v] * vl;
-      fr[v] = ur[v] * vr;
-    }
-    fl[d + 1] = fl[d + 1] + left[NV - 1];
-    fr[d + 1] = fr[d + 1] + right[NV - 1];
-    fl[NV - 1] = fl[NV - 1] + vl * left[NV - 1];
-    fr[NV - 1] = fr[NV - 1] + vr * right[NV - 1];
-    const R speed = np_max(fabs(vl) + sqrt((gl * left[NV - 1]) / left[0]),
-                           fabs(vr) + sqrt((gr * right[NV - 1]) / right[0]));
-    const R ar = area<R, DIM>(A, d, f, c);
-    R* W = A.W[d];
-    R flux0 = R(0);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      const R flux = ((fl[v] + fr[v]) - (ur[v] - ul[v]) * speed) * R(0.5);
-      if (v == 0) flux0 = flux;
-      W[v * nf + idx] = flux * ar;
-    }
-    // first-order upwind transport of the fractions (torchFiniteVolume.py:223-226)
-    for (int q = 0; q < A.nfrac; ++q) {
-      const R up = flux0 >= R(0) ? cl.q[q] : cr.q[q];
-      A.T[d][q * nf + idx] = (flux0 * up) * ar;
-    }
+    emit_face<R, DIM, D>(A, f, c, idx, cl, cr, sl, sr);
   }
   if (err) atomicOr(A.err, err);
 }
@@ -445,6 +459,82 @@ __device__ __forceinline__ int64_t face_off(int d, int f, const MIdx& c, const i
   if (d == 0) return ((int64_t)c.k * n[1] + c.j) * (n[0] + 1) + f;
   if (d == 1) return ((int64_t)c.k * (n[1] + 1) + f) * n[0] + c.i;
   return ((int64_t)f * n[1] + c.j) * n[0] + c.i;
+}
+
+// Faces of direction D (y or z) marched in chunks of `chunk` along D by one
+// thread each, threads adjacent along x: a sliding window of padded cells
+// f, f + 1, f + 2 and the slope of each padded cell formed once, so a face
+// costs one new cell load, one slope and one flux.  The values are those of
+// metric_face_kernel.
+template <typename R, int DIM, int D>
+__global__ void __launch_bounds__(kMThreads) metric_face_march_kernel(MArgs<R> A) {
+  const int chunk = A.chunk;
+  constexpr int NV = DIM + 2;
+  static_assert(D >= 1, "x faces use metric_face_kernel");
+  const int n = A.n[D];
+  const int nchunks = (n + chunk) / chunk;  // faces 0..n
+  const int64_t ntr = A.nc / n;             // cells of a plane normal to D
+  const int64_t total = ntr * nchunks;
+  const bool periodic = A.periodic[D];
+  int err = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t tr = t % ntr;
+    const int ch = (int)(t / ntr);
+    MIdx c;
+    c.i = (int)(tr % A.n[0]);
+    if (D == 1) {
+      c.j = 0;
+      c.k = (int)(tr / A.n[0]);
+    } else {
+      c.j = (int)(tr / A.n[0]);
+      c.k = 0;
+    }
+    const int f0 = ch * chunk;
+    const int f1 = min(f0 + chunk, n + 1);
+    MCell<R, NV> cl, cr, p;
+    R sl[NV], sr[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) sl[v] = sr[v] = R(0);
+    err |= padded_cell<R, NV, D>(A, f0, c, cl);
+    err |= padded_cell<R, NV, D>(A, f0 + 1, c, cr);
+    if (!A.first_order) {  // slope of padded cell f0
+      if (f0 >= 1) {
+        MCell<R, NV> m;
+        err |= padded_cell<R, NV, D>(A, f0 - 1, c, m);
+        cell_slope<R, NV>(m, cl, cr, A.limiter, sl);
+      } else if (periodic) {
+        MCell<R, NV> a, b, e;
+        err |= padded_cell<R, NV, D>(A, n - 1, c, a);
+        err |= padded_cell<R, NV, D>(A, n, c, b);
+        err |= padded_cell<R, NV, D>(A, n + 1, c, e);
+        cell_slope<R, NV>(a, b, e, A.limiter, sl);
+      }
+    }
+    for (int f = f0; f < f1; ++f) {
+      if (f + 2 <= n + 1) err |= padded_cell<R, NV, D>(A, f + 2, c, p);
+      if (!A.first_order) {  // slope of padded cell f + 1
+        if (f + 1 <= n) {
+          cell_slope<R, NV>(cl, cr, p, A.limiter, sr);
+        } else if (periodic) {
+          MCell<R, NV> a, b, e;
+          err |= padded_cell<R, NV, D>(A, 0, c, a);
+          err |= padded_cell<R, NV, D>(A, 1, c, b);
+          err |= padded_cell<R, NV, D>(A, 2, c, e);
+          cell_slope<R, NV>(a, b, e, A.limiter, sr);
+        } else {
+#pragma unroll
+          for (int v = 0; v < NV; ++v) sr[v] = R(0);
+        }
+      }
+      emit_face<R, DIM, D>(A, f, c, face_off(D, f, c, A.n), cl, cr, sl, sr);
+      cl = cr;
+      cr = p;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) sl[v] = sr[v];
+    }
+  }
+  if (err) atomicOr(A.err, err);
 }
 
 // -- 3. divergence and the SSPRK2 stage combination ---------------------------

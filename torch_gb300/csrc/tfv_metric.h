@@ -51,6 +51,7 @@ struct MFace {
 };
 
 constexpr int kMReduceBlocks = 512;  // fixed block count of every reduction (deterministic)
+constexpr int kMChunk = 32;          // longest run of y / z faces marched by one thread
 
 template <typename R>
 struct MArgs {
@@ -62,6 +63,7 @@ struct MArgs {
   int32_t limiter;    // 0 VanLeer, 1 Albada, 2 MINBEE, 3 Superbee, 4 Unos
   int32_t geometry;
   int32_t first_order;
+  int32_t chunk;      // y / z faces per thread of the marching face kernel
   int32_t znd;
   double gamma;
   R gam;              // gamma in the arithmetic type

@@ -204,7 +204,19 @@ struct Driver {
       int r = prim(v, slot_source);
       if (r) return r;
     }
-    for (int d = 0; d < m->dim; ++d) TFV_MCUDA(launch(kMOpFace, d, grid_for(m, m->nf[d])));
+    for (int d = 0; d < m->dim; ++d) {
+      // x faces: one thread per face; y and z faces: one thread per run of
+      // A.chunk faces, the run as long as keeps eight 256-thread CTAs per SM busy
+      int64_t work = m->nf[0];
+      if (d > 0) {
+        const int64_t lines = m->nc / m->cfg.n[d], faces = m->cfg.n[d] + 1;
+        const int64_t target = (int64_t)m->sms * 8 * 256;
+        A.chunk = (int)std::max<int64_t>(
+            4, std::min<int64_t>(kMChunk, (faces * lines + target - 1) / target));
+        work = lines * ((faces + A.chunk - 1) / A.chunk);
+      }
+      TFV_MCUDA(launch(kMOpFace, d, grid_for(m, work)));
+    }
     int64_t plane = 0;
     for (int d = 0; d < m->dim; ++d) plane = std::max<int64_t>(plane, m->nc / m->cfg.n[d]);
     const int g = reduce_grid(plane);
