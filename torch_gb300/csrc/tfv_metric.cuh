@@ -538,7 +538,8 @@ __global__ void __launch_bounds__(kMThreads) metric_face_march_kernel(MArgs<R> A
 }
 
 // -- 3. divergence and the SSPRK2 stage combination ---------------------------
-// stage 1: Uout = U + dt K, fractions (rho q + dt KQ) / rho_out.
+// stage 1: Uout = U + dt K, fractions (rho q + dt KQ) / rho_out, with KQ the
+//          fraction divergence of the transport arrays T.
 // stage 2: Uout = 0.5 (U0 + Us + dt K), fractions
 //          0.5 (rho0 q0 + rho_s q_s + dt KQ) / rho_out  (torchFiniteVolume.py:234-276)
 template <typename R, int DIM>

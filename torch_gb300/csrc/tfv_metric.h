@@ -84,7 +84,6 @@ struct MArgs {
   R* P;               // primitives [nv][nc]
   R* G;               // gamma [nc] (reactive)
   R* K;               // d state / dt [nv][nc]
-  R* KQ;              // d (rho q) / dt [nfrac][nc]
   R* W[3];            // area-weighted fluxes per direction [nv][nf]
   R* T[3];            // area-weighted fraction transport per direction [nfrac][nf]
   R* Uout;

@@ -32,9 +32,6 @@ constexpr int kSlotSource1 = 0, kSlotOutward1 = 1, kSlotSource2 = 2, kSlotOutwar
 
 size_t mal(size_t x) { return (x + 255) / 256 * 256; }
 
-// Step outcome of one SSPRK2 attempt
-enum { kStageOk = 0, kStageRetry = 1 };
-
 }  // namespace
 
 struct tfv_metric {
@@ -46,7 +43,7 @@ struct tfv_metric {
   size_t esz = 8;
   // workspace offsets (bytes)
   size_t off_state_a = 0, off_q_a[2] = {0, 0}, off_state_b = 0, off_q_b[2] = {0, 0};
-  size_t off_p = 0, off_g = 0, off_k = 0, off_kq = 0, off_w[3] = {0, 0, 0}, off_t[3] = {0, 0, 0};
+  size_t off_p = 0, off_g = 0, off_k = 0, off_w[3] = {0, 0, 0}, off_t[3] = {0, 0, 0};
   size_t off_faces = 0, off_fac = 0, off_part = 0, off_res = 0, off_rate = 0, off_err = 0, ws_size = 0;
   unsigned char* ws = nullptr;
   void* ring[2] = {nullptr, nullptr};
@@ -132,7 +129,6 @@ MArgs<R> make_args(const tfv_metric* m) {
   A.P = reinterpret_cast<R*>(m->ws + m->off_p);
   A.G = reinterpret_cast<R*>(m->ws + m->off_g);
   A.K = reinterpret_cast<R*>(m->ws + m->off_k);
-  A.KQ = reinterpret_cast<R*>(m->ws + m->off_kq);
   for (int d = 0; d < 3; ++d) {
     A.W[d] = reinterpret_cast<R*>(m->ws + m->off_w[d]);
     A.T[d] = reinterpret_cast<R*>(m->ws + m->off_t[d]);
@@ -192,7 +188,7 @@ struct Driver {
     prim_slot = slot;
     return reduce(slot, g);
   }
-  // one SSPRK2 right-hand side: K, KQ, the source and outward sums
+  // one SSPRK2 right-hand side: K, the face fluxes, the source and outward sums
   int rhs(const View& v, bool first_order, int slot_source, int slot_outward) {
     A.first_order = first_order ? 1 : 0;
     if (prim_state == v.u && prim_slot >= 0) {  // primitives of v already computed (dt pass)
@@ -482,7 +478,6 @@ int tfv_metric_create(int32_t precision, const tfv_metric_config* cfg, const dou
   m->off_p = take(st);
   m->off_g = take(sc);
   m->off_k = take(st);
-  m->off_kq = take(2 * sc);
   for (int d = 0; d < m->dim; ++d) {
     m->off_w[d] = take(m->esz * m->nv * m->nf[d]);
     m->off_t[d] = take(m->esz * 2 * m->nf[d]);
