@@ -140,6 +140,24 @@ def test_session_2d_explosion_cfl08_matches_oracle_bitwise():
     assert np.max(np.abs(gpu.balance_residual)) < 1e-12
 
 
+def test_full_size_2d_explosion_256_cfl08_to_t025_bitwise():
+    """The 2D explosion at its full size (256 x 256 on [0, 2]^2, VanLeer,
+    Open, CFL 0.8, to t = 0.25: 169 steps): every step's time and the final
+    state bit for bit against the oracle."""
+    prim = explosion_2d(256)
+    kw = dict(t_end=0.25, cfl=0.8, limiter="VanLeer", boundaries=["Open", "Open"],
+              strict_cfl=False)
+    gpu = torch_gb300.Simulation(prim, [2.0, 2.0], **kw)
+    ref = OracleSimulation(prim, [2.0, 2.0], **kw)
+    while not ref.completed:
+        ref.step()
+        gpu.step()
+        assert gpu.time == ref.time
+    assert gpu.steps == ref.steps == 169
+    np.testing.assert_array_equal(gpu.state, ref.state)
+    assert np.max(np.abs(gpu.balance_residual)) < 1e-12
+
+
 def test_session_3d_explosion_superbee_reflective_matches_oracle():
     prim = explosion_3d(24)
     kw = dict(t_end=1.0, cfl=0.6, limiter="Superbee", boundaries=["Reflective"] * 3,
