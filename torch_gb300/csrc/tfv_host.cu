@@ -652,7 +652,9 @@ static int create_internal(int32_t dim, int32_t precision, int32_t n, const tfv_
     // the fastest measured shape at 256^3)
     b->tile.tx = dim == 3 ? (precision == TFV_FP64 ? 32 : 16) : (dim == 2 ? 128 : 256);
     b->tile.ty = dim == 3 ? (precision == TFV_FP64 ? 4 : 16) : 1;
-    b->tile.chunk = dim == 3 ? 32 : 32;
+    // 3D FP32: 40-plane chunks (256^3: 1.065 ms per step kernel against 1.105
+    // with 32 and 1.085 with 48, measured)
+    b->tile.chunk = dim == 3 && precision == TFV_FP32 ? 40 : 32;
     b->tile.persistent_ctas = 0;
     b->tile.tma = 1;
   }
