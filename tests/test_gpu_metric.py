@@ -228,3 +228,27 @@ def test_inflow_and_pressure_outlet_on_every_face():
                     s.run()
                     np.testing.assert_allclose(s.state, initial, atol=1e-14, rtol=1e-14)
                     np.testing.assert_allclose(s.balance_residual, 0, atol=1e-13)
+
+
+def test_metric_max_steps_raise_and_keep_the_state():
+    sim, _ = start("m2d_cylindrical_origin", max_steps=2)
+    sim.step()
+    sim.step()
+    before, time = sim.state, sim.time
+    with pytest.raises(RuntimeError, match="Maximum steps"):
+        sim.step()
+    np.testing.assert_array_equal(sim.state, before)
+    assert sim.time == time and sim.steps == 2
+
+
+def test_reactive_metric_fp32_tracks_fp64():
+    name = "m3d_spherical_reactive"
+    s64, _ = start(name)
+    s32, _ = start(name, precision="fp32")
+    for _ in range(3):
+        s64.step()
+        s32.step()
+    rel = np.abs(s32.state - s64.state) / np.abs(s64.state).max(axis=(1, 2, 3))[:, None, None, None]
+    assert rel.mean() < 1e-5
+    assert np.mean(np.abs(s32.lam - s64.lam)) < 1e-5
+    assert abs(s32.time - s64.time) <= 1e-5 * s64.time
