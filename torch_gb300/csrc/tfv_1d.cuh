@@ -54,7 +54,7 @@ __device__ __forceinline__ void cell1(const InstDesc& d, const R* U, int k, R* u
 // (python/cfdSolver/torchSolver.py:1121-1122).
 template <typename R>
 __device__ __forceinline__ R gamma1(const InstDesc& d, const R* gam, int k) {
-  if (!gam) return R(d.gamma);
+  if (!gam) return desc_gamma(d, R(0));
   const int n = d.n[0];
   const int src = k < 0 ? (d.bc[0] == kBcPeriodic ? n - 1 : 0)
                         : (k >= n ? (d.bc[0] == kBcPeriodic ? 0 : n - 1) : k);

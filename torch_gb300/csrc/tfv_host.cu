@@ -269,6 +269,7 @@ void fill_desc(tfv_batch* b, int i) {
   d.max_steps = c.max_steps;
   d.cfl = c.cfl;
   d.gamma = c.gamma;
+  d.gamma_f = (float)c.gamma;
   d.t_end = c.t_end;
   d.q = c.q_heat;
   d.ea = c.activation;

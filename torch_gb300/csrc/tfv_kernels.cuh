@@ -294,7 +294,7 @@ __device__ __forceinline__ R fetch_padded(const InstDesc& d, const Geo<DIM>& g, 
   }
   const int64_t off = (int64_t)sp * g.ps + (int64_t)sb * g.na + sa;
   if (!TFV_IN(1, off, g.cs) || !TFV_IN(2, c, NV + 1)) return R(0);
-  if (c == NV) return gam ? gam[off] : R(d.gamma);
+  if (c == NV) return gam ? gam[off] : desc_gamma(d, R(0));
   R v = U[c * g.cs + off];
   if ((c == 1 && ga && g.bca == kBcReflective) ||
       (DIM == 3 && c == 2 && gb && g.bcb == kBcReflective) ||
@@ -627,7 +627,7 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   R* Un = (R*)d.U[dst];
   const R* gam = VARG ? (const R*)d.gam : nullptr;
   const double dt = st.dt;
-  const R gconst = R(d.gamma);
+  const R gconst = desc_gamma(d, R(0));
   (void)dt;
   R coefh[DIM], cu[DIM];
 #pragma unroll
@@ -1119,7 +1119,7 @@ __global__ void __launch_bounds__(256) fallback_kernel(StepArgs A) {
           u[c] = fetch_padded<R, DIM>(d, g, U, gam, c, a, b, p);
           un[c] = u[c];
         }
-        const R gc = VARG ? fetch_padded<R, DIM>(d, g, U, gam, NV, a, b, p) : R(d.gamma);
+        const R gc = VARG ? fetch_padded<R, DIM>(d, g, U, gam, NV, a, b, p) : desc_gamma(d, R(0));
 #pragma unroll
         for (int dd = 0; dd < DIM; ++dd) {
           const int ia = dd == 0 ? 1 : 0;
@@ -1237,7 +1237,7 @@ __global__ void __launch_bounds__(256) waves_kernel(StepArgs A, int sums) {
 #pragma unroll
           for (int c = 0; c < NV; ++c) sum[c] += (double)u[c];
         }
-        const R gc = VARG ? gam[off] : R(d.gamma);
+        const R gc = VARG ? gam[off] : desc_gamma(d, R(0));
         if (!physical_cell<R, NV>(u)) bad = true;
         R w[DIM];
         wave_speeds<R, DIM>(u, gc, w);
@@ -1381,10 +1381,21 @@ __device__ __forceinline__ R gamma_of_lambda(R lam) {
   return (R(4.5) - lam) / (R(3.5) - lam);
 }
 
+// Chemistry constants of an instance in the arithmetic type, converted once
+// per tile rather than per cell (a double-to-float conversion runs on the
+// narrow FP64 pipe).
 template <typename R>
-__device__ __forceinline__ R reaction_rate(const InstDesc& d, R lam, R s0, R s1, R s2) {
+struct Chem {
+  int closure;
+  R q, ea, a, gamma;
+  __device__ __forceinline__ explicit Chem(const InstDesc& d)
+      : closure(d.closure), q(R(d.q)), ea(R(d.ea)), a(R(d.a)), gamma(desc_gamma(d, R(0))) {}
+};
+
+template <typename R>
+__device__ __forceinline__ R reaction_rate(const Chem<R>& d, R lam, R s0, R s1, R s2) {
   const bool si = d.closure == 0;
-  const R g = si ? gamma_of_lambda(lam) : R(d.gamma);
+  const R g = si ? gamma_of_lambda(lam) : d.gamma;
   // uconsv_to_uprim (torchSolver.py:117-127)
   const R rho = np_max(s0, R(kFloor));
   const R u = s1 / rho;
@@ -1396,17 +1407,17 @@ __device__ __forceinline__ R reaction_rate(const InstDesc& d, R lam, R s0, R s1,
     const R molar = (lam * R(2.0 / 3.0)) * R(2.016) + (lam * R(1.0 / 3.0)) * R(32.0) +
                     (R(1) - lam) * R(18.016);
     t = np_max((p * molar) / (rho2 * R(8314.46)), R(kFloor));
-    return R(d.a) * texp(-R(d.ea) / (R(8.314) * t));
+    return d.a * texp(-d.ea / (R(8.314) * t));
   }
   t = np_max(p / rho, R(kFloor));
-  return R(d.a) * texp(-R(d.ea) / t);
+  return d.a * texp(-d.ea / t);
 }
 
 // One cell: returns false when the reference would reject the input
 // (reactant fraction outside [0,1] or not finite, nonphysical 1D state,
 // induction fraction outside [0,1]).
 template <typename R, int DIM>
-__device__ __forceinline__ bool react_cell(const InstDesc& d, R* u, R& lam, R& beta, bool znd,
+__device__ __forceinline__ bool react_cell(const Chem<R>& d, R* u, R& lam, R& beta, bool znd,
                                            double dt_r) {
   constexpr int NV = DIM + 2;
   const R s0 = u[0], s1 = u[1];
@@ -1421,7 +1432,7 @@ __device__ __forceinline__ bool react_cell(const InstDesc& d, R* u, R& lam, R& b
   ok = ok && finite_(s0) && finite_(s1) && finite_(s2) && s0 > R(kFloor) && e1 > R(kFloor);
   const R beta_n = znd ? beta : R(1);
   if (znd) ok = ok && finite_(beta) && beta >= R(0) && beta <= R(1);
-  const R q = R(d.q);
+  const R q = d.q;
   const R lam_n = lam;
   auto advance = [&](R rate, R duration, R& lam_out, R& beta_out) {
     if (znd) {
@@ -1476,6 +1487,7 @@ __global__ void __launch_bounds__(256) react_kernel(StepArgs A, int stage) {
     R* Bdst = znd ? (R*)d.beta[i1] : nullptr;
     R* gam = VARG ? (R*)d.gam : nullptr;
     const double half = 0.5 * st.dt;
+    const Chem<R> chem(d);
     const int ax = min(A.tx, g.na - T.x0);
     const int by = DIM == 3 ? min(A.ty, g.nb - T.y0) : 1;
     const bool owner = (int)threadIdx.x < ax * by;
@@ -1504,7 +1516,7 @@ __global__ void __launch_bounds__(256) react_kernel(StepArgs A, int stage) {
         }
         R lam = Lsrc[off];
         R beta = znd ? Bsrc[off] : R(1);
-        if (!react_cell<R, DIM>(d, u, lam, beta, znd, half)) fl |= kFlagChemistry;
+        if (!react_cell<R, DIM>(chem, u, lam, beta, znd, half)) fl |= kFlagChemistry;
         if (stage == 2) {
 #pragma unroll
           for (int c = 0; c < NV; ++c) {
@@ -1527,7 +1539,7 @@ __global__ void __launch_bounds__(256) react_kernel(StepArgs A, int stage) {
         for (int c = 0; c < NV; ++c) Udst[c * g.cs + off] = u[c];
         Ldst[off] = lam;
         if (znd) Bdst[off] = beta;
-        const R gc = (d.closure == 0) ? gamma_of_lambda(lam) : R(d.gamma);
+        const R gc = (chem.closure == 0) ? gamma_of_lambda(lam) : chem.gamma;
         if (VARG && stage == 1) gam[off] = gc;
         R w[DIM];
         wave_speeds<R, DIM>(u, gc, w);

@@ -580,8 +580,11 @@ __global__ void __launch_bounds__(kMThreads) metric_update_kernel(MArgs<R> A, in
         oq[q] = (R(0.5) * ((rho0 * A.Q0[q][off] + rhos * A.Qs[q][off]) + dt * kq[q])) / out[0];
     }
     if (!physical_cell<R, NV>(out)) err |= kMErrNonphysical;
+    // the reference's interval check (1e-12); single-precision roundoff of a
+    // fraction of exactly 1 needs a wider margin
+    const R tol = Exact<R>::value ? R(1e-12) : R(1e-5);
     for (int q = 0; q < A.nfrac; ++q) {
-      if (oq[q] < R(-1e-12) || oq[q] > R(1) + R(1e-12)) err |= kMErrFraction;
+      if (oq[q] < -tol || oq[q] > R(1) + tol) err |= kMErrFraction;
       oq[q] = np_min(np_max(oq[q], R(0)), R(1));  // np.clip
       A.Qout[q][off] = oq[q];
     }
@@ -711,6 +714,7 @@ __global__ void __launch_bounds__(kMThreads) metric_react_kernel(MArgs<R> A, int
   for (int v = 0; v < NV; ++v) part[v] = 0.0;
   int err = 0;
   const bool znd = A.znd;
+  const Chem<R> chem(A.chem);
   for (int64_t off = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; off < A.nc;
        off += (int64_t)gridDim.x * blockDim.x) {
     R u[NV], hyd[NV];
@@ -719,7 +723,7 @@ __global__ void __launch_bounds__(kMThreads) metric_react_kernel(MArgs<R> A, int
     for (int v = 0; v < NV; ++v) u[v] = hyd[v] = src[v * A.nc + off];
     R lam = mode == 0 ? A.Q[0][off] : A.Qout[0][off];
     R beta = znd ? (mode == 0 ? A.Q[1][off] : A.Qout[1][off]) : R(1);
-    if (!react_cell<R, DIM>(A.chem, u, lam, beta, znd, 0.5 * A.dt)) err |= kMErrChemistry;
+    if (!react_cell<R, DIM>(chem, u, lam, beta, znd, 0.5 * A.dt)) err |= kMErrChemistry;
     if (mode == 1) {
       const MIdx c = cell_of(off, A.n);
       const double vol = (double)volume<R, DIM>(A, c);

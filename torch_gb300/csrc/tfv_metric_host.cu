@@ -114,6 +114,7 @@ MArgs<R> make_args(const tfv_metric* m) {
   A.chem.a = m->cfg.a;
   A.chem.closure = 0;
   A.chem.gamma = m->cfg.gamma;
+  A.chem.gamma_f = (float)m->cfg.gamma;
   // factor arrays in the workspace: volume factors per axis, then face factors
   R* fac = reinterpret_cast<R*>(m->ws + m->off_fac);
   int64_t o = 0;

@@ -56,6 +56,14 @@ __device__ __forceinline__ R guarded(R x, R g) { return (fabs(x) < g) ? g : x; }
 template <typename R>
 __device__ __forceinline__ bool finite_(R x) { return isfinite(x); }
 
+// Constant gamma of an instance descriptor in the arithmetic type: single
+// precision reads its float copy instead of converting the double per cell
+// (a double-to-float conversion runs on the narrow FP64 pipe).
+template <typename D>
+__device__ __forceinline__ double desc_gamma(const D& d, double) { return d.gamma; }
+template <typename D>
+__device__ __forceinline__ float desc_gamma(const D& d, float) { return d.gamma_f; }
+
 // --------------------------------------------------------------------------
 // Limiters (LIM: 0 VanLeer, 1 Albada, 2 MINBEE, 3 Superbee, 4 Unos).
 // 3D: python/cfdSolver/torchSolver3D.py:86-111.

@@ -29,6 +29,8 @@ struct InstDesc {
   double h[3];
   double vol;            // hx*hy*hz over the active axes
   double cfl, gamma, t_end;
+  float gamma_f;         // gamma in single precision (no per-cell conversion)
+  int32_t pad_gamma;
   double q, ea, a;       // chemistry constants
   double inlet[4];       // conservative 2D inlet state (gamma 1.4)
   void* U[kMaxRing];
