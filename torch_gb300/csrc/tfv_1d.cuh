@@ -319,9 +319,14 @@ __global__ void __launch_bounds__(256) waves1d_kernel(StepArgs A, int in_step) {
 // Limited half-step states (left ol, right orr) of a cell with state c0
 // between neighbours cm and cp (python/cfdSolver/torchSolver.py:412-491).
 template <typename R>
-__device__ __forceinline__ void recon1_cells(const InstDesc& d, const InstState& st,
-                                             const R* c0, const R* cm, const R* cp, R g, R* ol,
-                                             R* orr) {
+__device__ __forceinline__ R recon1_coef(const InstDesc& d, const InstState& st) {
+  return -R(st.dt / (2.0 * d.h[0]));  // -(dt / (2 dx)) of the Hancock half step
+}
+
+// kcoef = recon1_coef(d, st), formed once per tile by the caller
+template <typename R>
+__device__ __forceinline__ void recon1_cells(const InstDesc& d, const R* c0, const R* cm,
+                                             const R* cp, R g, R kcoef, R* ol, R* orr) {
   R w = R(0);
   if (d.controller == 0) {  // Sound Speed Controlled
     R rho, v, p;
@@ -341,10 +346,9 @@ __device__ __forceinline__ void recon1_cells(const InstDesc& d, const InstState&
   R fl[3], fr[3];
   flux1(ul, g, fl);
   flux1(ur, g, fr);
-  const R k = -R(st.dt / (2.0 * d.h[0]));
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const R dfu = k * (fr[c] - fl[c]);
+    const R dfu = kcoef * (fr[c] - fl[c]);
     ol[c] = ul[c] + dfu;
     orr[c] = ur[c] + dfu;
   }
@@ -368,7 +372,7 @@ __device__ __forceinline__ void recon1(const InstDesc& d, const InstState& st, c
   cell1(d, U, i, c0);
   cell1(d, U, i - 1, cm);
   cell1(d, U, i + 1, cp);
-  recon1_cells<R>(d, st, c0, cm, cp, gamma1(d, gam, i), ol, orr);
+  recon1_cells<R>(d, c0, cm, cp, gamma1(d, gam, i), recon1_coef<R>(d, st), ol, orr);
 }
 
 // MUSCL reconstruction and half-step predictor per cell
@@ -577,6 +581,7 @@ __global__ void __launch_bounds__(256) step1d_kernel(StepArgs A) {
     const int ax = min(A.tx, n - T.x0);
     const int x0 = T.x0;
     const bool per = d.bc[0] == kBcPeriodic, refl = d.bc[0] == kBcReflective;
+    const R kcoef = recon1_coef<R>(d, st);
     // slot k <-> padded cell x0 - 3 + k
     for (int k = threadIdx.x; k < ax + 6; k += blockDim.x) {
       const int pk = x0 - 3 + k;
@@ -599,7 +604,7 @@ __global__ void __launch_bounds__(256) step1d_kernel(StepArgs A) {
         cm[c] = us[c * W + k - 1];
         cp[c] = us[c * W + k + 1];
       }
-      recon1_cells<R>(d, st, c0, cm, cp, gs[k], ol, orr);
+      recon1_cells<R>(d, c0, cm, cp, gs[k], kcoef, ol, orr);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         rc[c * W + k] = ol[c];
@@ -712,8 +717,9 @@ __global__ void __launch_bounds__(256) step1d_kernel(StepArgs A) {
     const int fl = block_or(bad ? kFlagNonphysical : 0, reinterpret_cast<int*>(red));
     const double mws = (double)block_max(ws, red);
     const double mwh = (double)block_max(wh, red);
-    double sm[3];
-    for (int c = 0; c < 3; ++c) sm[c] = block_sum(bsum[c], red);
+    double sm[3] = {0.0, 0.0, 0.0};
+    if (x0 == 0 || x0 + ax == n)  // boundary faces only in the end tiles (uniform)
+      for (int c = 0; c < 3; ++c) sm[c] = block_sum(bsum[c], red);
     if (threadIdx.x == 0) {
       A.t_wmax[(size_t)t * 3 + 0] = mws;
       A.t_wmax[(size_t)t * 3 + 1] = mwh;
