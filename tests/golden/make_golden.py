@@ -328,11 +328,15 @@ def checkpoint_cases(R):
     sys.modules["h5py"] = _RecordingHDF5("h5py")
     io = importlib.import_module("cfdSolver.torchIO")
     cases = session_setups(R)
+    metric = metric_setups(R)
+    for name in ("m2d_cylindrical_origin", "m3d_cartesian_faces", "m2d_spherical_reactive"):
+        cases[name] = metric[name]
     out = {}
     with tempfile.TemporaryDirectory() as tmp:
         for name in ("s3d_explosion", "s3d_open_albada", "s2d_explosion", "s1d_sod",
                      "s3d_ignition_znd", "s3d_ignition_arr", "s2d_reactive",
-                     "s1d_reactive_znd"):
+                     "s1d_reactive_znd", "m2d_cylindrical_origin", "m3d_cartesian_faces",
+                     "m2d_spherical_reactive"):
             s = cases[name]
             # a later end time so that all 8 steps run (the session reads it each step)
             s.config["t_end"] = 1e-3 if s.config["reactive"] else 1.0

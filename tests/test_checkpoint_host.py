@@ -1,6 +1,6 @@
 """Checkpoint interchange on the host: the reference's own checkpoints
 (written by python/cfdSolver/torchIO.py write_checkpoint after 4 steps of
-seeded sessions, tests/golden/make_golden.py) parse into snapshots that
+seeded Cartesian and metric sessions, tests/golden/make_golden.py) parse into snapshots that
 re-encode byte for byte, corrupt files are rejected like the reference's
 reader rejects them (python/tests/testSession.py:55-79, 192-261), and files
 are replaced atomically.  h5py is not installed, so an npz-backed stand-in
@@ -16,7 +16,8 @@ from torch_gb300 import checkpoint
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 CASES = ("s3d_explosion", "s3d_open_albada", "s2d_explosion", "s1d_sod", "s3d_ignition_znd",
-         "s3d_ignition_arr", "s2d_reactive", "s1d_reactive_znd")
+         "s3d_ignition_arr", "s2d_reactive", "s1d_reactive_znd", "m2d_cylindrical_origin",
+         "m3d_cartesian_faces", "m2d_spherical_reactive")
 
 
 def reference_checkpoint(name):

@@ -6,7 +6,9 @@ the reference reader's checks; and a restart from a checkpoint is exact in
 every dimension and chemistry model (python/tests/testSession.py:81-126).
 Inert FP64 results are compared bitwise; reactive ones at the relative
 tolerance 1e-10 of the reactive parity tests (CUDA's and NumPy's exp differ
-in the last bit)."""
+in the last bit).  The metric sessions among them (a cylindrical grid with a
+wall at the origin, a Cartesian grid with per-face boundaries, a reactive
+spherical shell) resume on the metric engine."""
 
 import json
 from pathlib import Path
@@ -26,7 +28,8 @@ from oracle.session import OracleSimulation  # noqa: E402
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 CASES = ("s3d_explosion", "s3d_open_albada", "s2d_explosion", "s1d_sod", "s3d_ignition_znd",
-         "s3d_ignition_arr", "s2d_reactive", "s1d_reactive_znd")
+         "s3d_ignition_arr", "s2d_reactive", "s1d_reactive_znd", "m2d_cylindrical_origin",
+         "m3d_cartesian_faces", "m2d_spherical_reactive")
 
 
 def golden(name):
