@@ -37,15 +37,19 @@ def test_struct_layouts_match_c(tmp_path):
     src = tmp_path / "sizes.c"
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "tfv.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu\\n\", sizeof(tfv_config),"
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(tfv_config),"
         " sizeof(tfv_tile), sizeof(tfv_report), offsetof(tfv_config, spacing),"
-        " offsetof(tfv_report, steps));return 0;}\n")
+        " offsetof(tfv_report, steps), sizeof(tfv_metric_face), sizeof(tfv_metric_config),"
+        " offsetof(tfv_metric_config, max_steps), offsetof(tfv_metric_config, faces));"
+        "return 0;}\n")
     exe = tmp_path / "sizes"
     subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
                                           check=True).stdout.split()]
     assert got == [C.sizeof(_lib.Config), C.sizeof(_lib.Tile), C.sizeof(_lib.Report),
-                   _lib.Config.spacing.offset, _lib.Report.steps.offset]
+                   _lib.Config.spacing.offset, _lib.Report.steps.offset,
+                   C.sizeof(_lib.MetricFace), C.sizeof(_lib.MetricConfig),
+                   _lib.MetricConfig.max_steps.offset, _lib.MetricConfig.faces.offset]
 
 
 def test_invalid_arguments_are_rejected_without_a_gpu():
@@ -83,3 +87,34 @@ def test_precision_units_share_no_mergeable_symbols():
         for unit in ("tfv_f32_2d.cu", "tfv_f32_3d.cu", "tfv_metric_f32.cu"):
             shared = f64 & _weak_symbols(objs[unit])
             assert not shared, (double_unit, unit, sorted(shared)[:5])
+
+
+def test_metric_and_rusanov_arguments_are_rejected_without_a_gpu():
+    lib = _lib.load()
+    cfg = _lib.MetricConfig()
+    cfg.dim = 2
+    cfg.n[0], cfg.n[1] = 8, 4
+    cfg.lengths[0], cfg.lengths[1] = 1.0, 1.0
+    cfg.geometry = _lib.GEOMETRIES["annular"]
+    cfg.cfl, cfg.gamma, cfg.t_end, cfg.max_steps = 0.4, 1.4, 1.0, 10
+    cfg.faces[2].type = _lib.FACE_TYPES["periodic"]  # y_min periodic, y_max not
+    count = lib.tfv_metric_factor_count(C.byref(cfg))
+    assert count == 8 + 4 + (9 + 4) + (8 + 5)
+    factors = (C.c_double * count)(*([1.0] * count))
+    handle = C.c_void_p()
+    code = lib.tfv_metric_create(_lib.TFV_FP64, C.byref(cfg), factors, C.byref(handle))
+    assert code == _lib.TFV_EINVAL and "Periodic" in _lib.last_error()
+    cfg.faces[2].type = _lib.FACE_TYPES["outflow"]
+    cfg.dim = 4
+    assert lib.tfv_metric_create(_lib.TFV_FP64, C.byref(cfg), factors,
+                                 C.byref(handle)) == _lib.TFV_EINVAL
+    cfg.dim = 2
+    code = lib.tfv_metric_create(_lib.TFV_FP64, C.byref(cfg), factors, C.byref(handle))
+    assert code == _lib.TFV_OK  # a valid configuration needs no device until bind
+    size = C.c_size_t()
+    assert lib.tfv_metric_workspace_size(handle, C.byref(size)) == _lib.TFV_OK and size.value > 0
+    lib.tfv_metric_destroy(handle)
+    assert lib.tfv_rusanov_flux(0, 6, 10, 0, None, None, None, None, None,
+                                None) == _lib.TFV_EINVAL
+    assert lib.tfv_rusanov_flux(0, 4, 10, 2, None, None, None, None, None,
+                                None) == _lib.TFV_EINVAL
