@@ -223,17 +223,23 @@ int tfv_hydro_step(const tfv_config* cfg, int32_t precision, const void* state_i
  * application that owns all GPU memory in a pool of its own and hands this
  * library only the state and flux arrays, or a time-critical loop where the
  * device-wide synchronisation an allocation implies is not acceptable.
- * The step's scratch (descriptors, tile table, per-tile partial sums) lives
- * in a 1 MiB array inside the library's device image; every GPU that loads
- * the library holds it until the process exits.  Grids whose scratch would
- * not fit are rejected with TFV_EINVAL (the limit is about 4,900 tiles: a
- * 3D 256^3 grid needs 218 KiB in fp32 and 435 KiB in fp64).  The first call
- * on a device looks the array's address up (cudaGetSymbolAddress) with that
- * device current; make that first call before any stream capture.  Every
- * call reuses the same array: a call rewrites the descriptors, tile table and
- * scalars (the fallback flag starts at zero) and every partial sum before
- * reading them, but calls that overlap on the GPU (other streams, other host
- * threads) race on the array and must be serialised by the caller. */
+ * The step's scratch (descriptors, tile table, per-tile partial sums, and
+ * per-cell interface data of 1D tubes) lives in a 1 MiB array inside the
+ * library's device image; every GPU that loads the library holds it until the
+ * process exits.  Grids whose scratch would not fit are rejected with
+ * TFV_EINVAL; tfv_step_workspace_size gives a grid's need (with the default
+ * tiles a 3D 256^3 grid needs about 376 KiB in fp32 and 856 KiB in fp64, so
+ * fp64 3D grids much larger than 256^3 are rejected; a 2D 4096^2 grid needs
+ * 856 KiB; 1D tubes need about 49 B per cell in fp32 and 97 B in fp64, so
+ * tubes beyond about 21,000 / 10,800 cells are rejected).  The array's device
+ * address is looked up (cudaGetSymbolAddress) on every call with the calling
+ * thread's device current.  The call blocks until the step has finished (it
+ * reads the step's status back to the host), so it cannot be used on a
+ * capturing stream.  Every call reuses the same array: a call rewrites the
+ * descriptors, tile table and scalars (the fallback flag starts at zero) and
+ * every partial sum before reading them, but calls that overlap on the GPU
+ * (other streams, other host threads) race on the array and must be
+ * serialised by the caller. */
 int tfv_hydro_step_static(const tfv_config* cfg, int32_t precision, const void* state_in,
                           void* state_out, const void* gamma_cells, double dt, void* fx,
                           void* fy, void* fz, int32_t* used_fallback, void* stream);

@@ -1,9 +1,10 @@
 """Generate golden vectors by running the TORCH reference itself.
 
-Run in a container that has the reference source tree (default
-``/root/reference``, or ``$TORCH_REFERENCE``):
+Run where the reference source tree is available, naming its root (the
+directory that holds ``python/cfdSolver``) with ``--reference`` or
+``$TORCH_REFERENCE``:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference PATH [checkpoint|metric|rusanov|output]
 
 The reference package ``cfdSolver`` imports matplotlib at package level, so it
 is loaded through a bare namespace module whose ``__path__`` points at the
@@ -22,7 +23,7 @@ from pathlib import Path
 import numpy as np
 
 OUT = Path(__file__).resolve().parent
-REF = Path(os.environ.get("TORCH_REFERENCE", "/root/reference")) / "python"
+REF = None  # <reference root>/python, set by main()
 
 
 def load_reference():
@@ -681,18 +682,25 @@ def exact_riemann_cases():
 
 
 def main():
+    import argparse
+
+    global REF
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--reference", default=os.environ.get("TORCH_REFERENCE"),
+                    help="root of the TORCH source tree (default: $TORCH_REFERENCE)")
+    ap.add_argument("case", nargs="?", choices=["checkpoint", "metric", "rusanov", "output"],
+                    help="regenerate this fixture alone")
+    args = ap.parse_args()
+    if not args.reference:
+        ap.error("name the reference source tree with --reference or $TORCH_REFERENCE")
+    REF = Path(args.reference) / "python"
+    if not (REF / "cfdSolver").is_dir():
+        ap.error(f"{REF / 'cfdSolver'} is not a directory")
     R = load_reference()
-    if sys.argv[1:] == ["checkpoint"]:  # regenerate checkpoint.npz alone
-        checkpoint_cases(R)
-        return
-    if sys.argv[1:] == ["metric"]:  # regenerate metric.npz alone
-        metric_cases(R)
-        return
-    if sys.argv[1:] == ["rusanov"]:  # regenerate rusanov.npz alone
-        rusanov_cases(R)
-        return
-    if sys.argv[1:] == ["output"]:  # regenerate output.npz alone
-        output_cases(R)
+    single = {"checkpoint": checkpoint_cases, "metric": metric_cases,
+              "rusanov": rusanov_cases, "output": output_cases}
+    if args.case:
+        single[args.case](R)
         return
     rng = np.random.default_rng(20261203)
     hllc_cases(R, rng)

@@ -27,7 +27,7 @@ def candidates(dim, precision, sms):
     if dim == 3:
         shapes = [(16, 16), (32, 8)] if precision == "fp32" else [(32, 4), (16, 8)]
         for tx, ty in shapes:
-            for chunk in (16, 32, 64):
+            for chunk in (16, 32, 40, 64):
                 out.append((tx, ty, chunk, 0, 1))
     elif dim == 2:
         for tx in (128, 256):

@@ -1105,25 +1105,17 @@ namespace {
 
 constexpr size_t kStaticScratchBytes = size_t(1) << 20;  // 1 MiB on every device
 __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
-std::mutex g_static_mutex;
-constexpr int kMaxDevices = 256;
-void* g_static_ptr[kMaxDevices] = {};
 
-// Device address of g_static_scratch on the current device.  Host code may
-// not use the symbol itself (it names a host-side shadow); the address is
-// looked up once per device, with that device current.
+// Device address of g_static_scratch in the current device's context.  Host
+// code may not use the symbol itself (it names a host-side shadow).  The
+// address is looked up on every call, with the device current: the lookup is
+// a table read in the CUDA runtime, and a cached address would go stale when
+// the context is torn down and re-created (cudaDeviceReset).
 int static_scratch(void** out) {
-  int dev = 0;
-  TFV_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return fail(TFV_EINVAL, "device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_static_mutex);
-  if (!g_static_ptr[dev]) {
-    void* p = nullptr;
-    TFV_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
-    if (!p) return fail(TFV_ECUDA, "cudaGetSymbolAddress returned a null address");
-    g_static_ptr[dev] = p;
-  }
-  *out = g_static_ptr[dev];
+  void* p = nullptr;
+  TFV_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
+  if (!p) return fail(TFV_ECUDA, "cudaGetSymbolAddress returned a null address");
+  *out = p;
   return TFV_OK;
 }
 
