@@ -11,9 +11,10 @@ larger than L2, so no flush is needed between steps.
 
 With --gpus N > 1 (torchrun) every rank advances its own grid ("replicas
 only": the step has no cross-rank exchange); value = total cell updates of
-all ranks / max rank time.  --impl reference times the reference algorithm's
-CPU implementation (the NumPy restatement in oracle/, threaded HLLC batches
-like the reference's Execution pool) on a bounded slab of the same workload.
+all ranks / max rank time.  --impl reference times the reference's own CPU
+step (its Simulation.step() from baseline/_ref, HLLC batches on every host
+core through its Execution pool; the oracle's NumPy restatement where the
+reference is not installed) on a bounded slab of the same workload.
 """
 
 import argparse
@@ -121,30 +122,181 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def reference_modules():
+    """The reference's own modules from baseline/_ref (installed there by
+    baseline/install_reference.py), or None when it is not installed.  The
+    package's __init__ imports matplotlib, which the step does not need, so
+    the modules are loaded through a bare namespace package whose path is the
+    installed package directory."""
+    import importlib
+    import types
+
+    base = os.path.join(ROOT, "baseline", "_ref", "cfdSolver")
+    if not os.path.isfile(os.path.join(base, "torchSession.py")):
+        return None
+    pkg = types.ModuleType("cfdSolver")
+    pkg.__path__ = [base]
+    sys.modules["cfdSolver"] = pkg
+    return types.SimpleNamespace(session=importlib.import_module("cfdSolver.torchSession"))
+
+
 def cpu_reference(steps, warmup, nz=16, workers=1):
-    """The reference algorithm on the host: NumPy restatement, central z-slab
-    (256 x 256 x nz) of the explosion with reflective walls."""
-    from oracle import fv
+    """The reference's CPU step on a central z-slab (256 x 256 x nz) of the
+    headline workload, reflective walls, Superbee, CFL 0.6.
 
-    fv.set_workers(workers)
+    Where the reference is installed it is its own Simulation.step() (the
+    session's CFL dt, torchSolver3D._hydro with HLLC batches on `workers`
+    threads of its Execution pool, and the conservation audit): the session is
+    built at CFL 0.5, the largest its validation accepts, and the CFL is set to
+    0.6 in its config afterwards (the step arithmetic reads it only for dt).
+    Otherwise it is the oracle's NumPy restatement of the same step.  Returns
+    the median cell-updates/s of `steps` individually timed steps after
+    `warmup`, the per-step samples in ms, the sample description and kind."""
     prim = explosion_3d(N, nz)
-    state = fv.prim_to_cons(prim, 1.4)
-    h = (1.0 / N,) * 3
-    bcs = ["Reflective"] * 3
+    R = reference_modules()
+    if R is not None:
+        sess = R.session.Simulation(prim, [1.0, 1.0, nz / N], t_end=1e9, cfl=0.5, gamma=1.4,
+                                    boundaries=["Reflective"] * 3, limiter="Superbee",
+                                    max_steps=10 ** 9, workers=workers)
+        sess.config["cfl"] = 0.6
+        one, kind = sess.step, "reference"
+        what = "the reference's Simulation.step() (baseline/_ref)"
+    else:
+        from oracle import fv
 
-    def one(s):
-        dt = fv.dt_3d(s, h, 0.6, 1.4)
-        return fv.hydro_3d(s, 1.4, h, dt, "Superbee", bcs)[0]
+        fv.set_workers(workers)
+        box = {"u": fv.prim_to_cons(prim, 1.4)}
+        h = (1.0 / N,) * 3
 
+        def one():
+            u = box["u"]
+            dt = fv.dt_3d(u, h, 0.6, 1.4)
+            box["u"] = fv.hydro_3d(u, 1.4, h, dt, "Superbee", ["Reflective"] * 3)[0]
+
+        kind, what = "port", "the oracle's NumPy restatement"
     for _ in range(warmup):
-        state = one(state)
+        one()
     samples = []
     for _ in range(steps):
         t0 = time.perf_counter()
-        state = one(state)
-        samples.append(time.perf_counter() - t0)
+        one()
+        samples.append((time.perf_counter() - t0) * 1e3)
+    if R is not None:
+        sess.close()
     cells = N * N * nz
-    return cells / statistics.median(samples), f"{N}x{N}x{nz} central z-slab, median of {steps} steps"
+    ms = statistics.median(samples)
+    sample = (f"{what} on a {N}x{N}x{nz} central z-slab, {workers} worker thread(s), "
+              f"median of {steps} steps after {warmup}")
+    return cells / (ms * 1e-3), samples, sample, kind
+
+
+def gpu_numa_node(index):
+    """NUMA node that sysfs gives for the GPU's PCI device, or None."""
+    try:
+        bus = subprocess.run(["nvidia-smi", "-i", str(index), "--query-gpu=pci.bus_id",
+                              "--format=csv,noheader"], capture_output=True, text=True,
+                             timeout=30).stdout.strip()
+        dom, rest = bus.split(":", 1)
+        path = f"/sys/bus/pci/devices/{dom[-4:].lower()}:{rest.lower()}/numa_node"
+        node = int(open(path).read().strip())
+        return node if node >= 0 else None
+    except (OSError, ValueError, subprocess.SubprocessError):
+        return None
+
+
+def node_cpus(node):
+    """CPUs of a NUMA node (sysfs cpulist), as a set."""
+    try:
+        text = open(f"/sys/devices/system/node/node{node}/cpulist").read().strip()
+    except OSError:
+        return set()
+    cpus = set()
+    for part in filter(None, text.split(",")):
+        a, _, b = part.partition("-")
+        cpus.update(range(int(a), int(b or a) + 1))
+    return cpus
+
+
+def pages_by_node(ptr):
+    """NUMA nodes of the pages of the mapping that holds host address `ptr`
+    (/proc/self/numa_maps: {node: pages})."""
+    best, counts = -1, {}
+    try:
+        for line in open("/proc/self/numa_maps"):
+            fields = line.split()
+            start = int(fields[0], 16)
+            if best < start <= ptr:
+                best = start
+                counts = {int(f[1:f.index("=")]): int(f[f.index("=") + 1:])
+                          for f in fields[2:] if f[0] == "N" and "=" in f}
+    except (OSError, ValueError):
+        return {}
+    return counts
+
+
+class near_gpu_memory:
+    """Host allocations made inside this block land on the GPU's nearest NUMA
+    node: the process runs only on that node's CPUs (those it may use) while
+    the block is open, and pinned pages are placed where the allocating
+    thread runs."""
+
+    def __init__(self, index):
+        self.node = gpu_numa_node(index)
+        self.saved = None
+
+    def __enter__(self):
+        if self.node is not None and hasattr(os, "sched_setaffinity"):
+            allowed = os.sched_getaffinity(0)
+            mine = node_cpus(self.node) & allowed
+            if mine and mine != allowed:
+                self.saved = allowed
+                os.sched_setaffinity(0, mine)
+        return self
+
+    def __exit__(self, *exc):
+        if self.saved is not None:
+            os.sched_setaffinity(0, self.saved)
+
+
+def link_rates(host_in, dev, host_out, reps=3):
+    """GB/s of the host link for one buffer: host-to-device alone,
+    device-to-host alone, and both directions at once (two streams)."""
+    import torch
+
+    nbytes = dev.numel() * dev.element_size()
+    up, down = torch.cuda.Stream(), torch.cuda.Stream()
+    spare = torch.empty_like(dev)
+
+    def best(fn):
+        ms = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            up.wait_stream(torch.cuda.current_stream())
+            down.wait_stream(torch.cuda.current_stream())
+            fn()
+            torch.cuda.current_stream().wait_stream(up)
+            torch.cuda.current_stream().wait_stream(down)
+            b.record()
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        return min(ms)
+
+    def h2d():
+        with torch.cuda.stream(up):
+            spare.copy_(host_in, non_blocking=True)
+
+    def d2h():
+        with torch.cuda.stream(down):
+            host_out.copy_(dev, non_blocking=True)
+
+    t_up, t_down = best(h2d), best(d2h)
+    t_both = best(lambda: (h2d(), d2h()))
+    del spare
+    return {"h2d_gbs": nbytes / (t_up * 1e-3) / 1e9, "d2h_gbs": nbytes / (t_down * 1e-3) / 1e9,
+            "both_gbs": 2 * nbytes / (t_both * 1e-3) / 1e9,
+            "floor_ms_per_session_step": t_both}
 
 
 def max_over_ranks(ms, dist, device=None):
@@ -180,6 +332,73 @@ def _timed(stream, fn):
     return a.elapsed_time(b)
 
 
+def pressure(u, gamma):
+    """Pressure of a conserved state (rho, m..., E) in double precision."""
+    u = u.double()
+    kinetic = 0.5 * sum(u[k] * u[k] for k in range(1, u.shape[0] - 1)) / u[0]
+    return (gamma - 1.0) * (u[-1] - kinetic)
+
+
+def compare_precisions(s32, s64, gamma):
+    """L1 (mean) and L-infinity differences of density and pressure of an
+    FP32 session against the FP64 session of the same workload after the same
+    steps, their relative L1 (sum |diff| / sum |FP64|), and the conservation
+    drift of each: balance residual relative to the initial integrals, and the
+    FP32 integrals relative to the FP64 ones."""
+    u32, u64 = s32.device_state.double(), s64.device_state.double()
+    out = {}
+    for name, a, b in (("rho", u32[0], u64[0]),
+                       ("p", pressure(u32, gamma), pressure(u64, gamma))):
+        d = (a - b).abs()
+        out["l1_" + name] = float(d.mean())
+        out["linf_" + name] = float(d.max())
+        out["rel_l1_" + name] = float(d.sum() / b.abs().sum())
+    scale = lambda s: np.maximum(np.abs(s.initial_integral), 1e-300)
+    for tag, s in (("fp32", s32), ("fp64", s64)):
+        out[tag + "_balance_rel"] = float(np.max(np.abs(s.balance_residual)
+                                                 / np.maximum(np.abs(s.initial_integral), 1.0)))
+        out[tag + "_balance_rel_per_var"] = (np.abs(s.balance_residual) / scale(s)).tolist()
+    i32, i64 = s32.integral, s64.integral
+    out["fp32_integral_rel_to_fp64"] = (np.abs(i32 - i64)
+                                        / np.maximum(np.abs(i64), 1e-300)).tolist()
+    out["time_fp32"], out["time_fp64"] = s32.time, s64.time
+    out["steps_fp32"], out["steps_fp64"] = s32.steps, s64.steps
+    return out
+
+
+def accuracy_leg(prim, kw, n, steps=200, warmup=2, graph_steps=10):
+    """The headline workload advanced `steps` steps in FP32 and in plain FP64
+    (both timed over the steps after `warmup`), then compared."""
+    import torch
+
+    import torch_gb300
+
+    out = {"workload": f"3D spherical explosion {n}^3, Superbee, reflective, CFL 0.6, "
+                       f"{steps} steps in FP32 and in FP64 from the same initial state"}
+    sims = {}
+    for prec in ("fp32", "fp64"):
+        sim = torch_gb300.Simulation(prim, [1, 1, 1], precision=prec, graph_steps=graph_steps,
+                                     **kw)
+        sim.advance(warmup)
+        sim.synchronize()
+        ms = _timed(sim._engine.stream, lambda: sim.advance(steps - warmup)) / (steps - warmup)
+        sim.synchronize()
+        sim._engine.refresh()
+        bpc = BYTES_PER_CELL[prec]
+        out[prec] = {"value": n ** 3 / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+                     "timed_steps": steps - warmup, "steps": sim.steps,
+                     "fallback_steps": sim.fallback_steps,
+                     "hbm_gbs_at_algorithmic_bytes": bpc * n ** 3 / (ms * 1e-3) / 1e9}
+        sims[prec] = sim
+    out["fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    out.update(compare_precisions(sims["fp32"], sims["fp64"], kw.get("gamma", 1.4)))
+    for sim in sims.values():
+        sim.close()
+    del sims
+    torch.cuda.empty_cache()
+    return out
+
+
 def ignition_3d(n):
     """Nondimensional ignition: rho = 1, T = 1 + 2 exp(-r^2 / (2 * 0.05^2)),
     p = rho T, at rest, reactant fraction 1."""
@@ -192,46 +411,69 @@ def ignition_3d(n):
     return p
 
 
-def reactive_leg(n=192, steps=20, warmup=3):
+def reactive_leg(n=192, steps=300, warmup=3):
     """3D reactive ignition, single-step Arrhenius (nondimensional: A = 1e3,
     Ea/R = 25, q = 20, gamma = 1.2), Van Albada, open boundaries, CFL 0.4:
-    FP32 with FP64 sums against the FP64 plain path after the same steps."""
+    FP32 with FP64 sums against the FP64 plain path, each advanced until
+    `steps` steps have committed (an attempt whose reaction half step halves
+    dt commits nothing, as in the reference), then compared.  The
+    nondimensional closure has no implementation in the reference: its parity
+    is against the oracle's restatement only."""
+    import torch
+
     import torch_gb300
 
     prim = ignition_3d(n)
-    kw = dict(t_end=1e9, cfl=0.4, gamma=1.2, reactive=True, limiter="Albada",
+    gamma = 1.2
+    kw = dict(t_end=1e9, cfl=0.4, gamma=gamma, reactive=True, limiter="Albada",
               max_steps=10 ** 9, chemistry=dict(closure="nondimensional", q_heat=20.0,
                                                 activation_energy=25.0, pre_exponential=1e3))
     out = {"workload": f"3D reactive ignition {n}^3, nondimensional Arrhenius, Van Albada, "
-                       f"open, CFL 0.4; {steps} timed step attempts after {warmup} "
-                       "(a reactive dt halving is an attempt that commits nothing; rates "
-                       "count committed steps)"}
+                       f"open, CFL 0.4; {steps} committed steps, the last {steps - warmup} "
+                       "timed (rates count committed steps; attempts that halved dt are "
+                       "inside the timed region)",
+           "parity": "unpinned (the closure has no reference implementation; checked "
+                     "against the oracle's restatement)"}
     sims = {}
     for prec in ("fp32", "fp64"):
         sim = torch_gb300.Simulation(prim, [1, 1, 1], precision=prec, graph_steps=1, **kw)
-        sim.advance(warmup)
-        sim.synchronize()
-        sim._engine.refresh()
+
+        def until(target):
+            attempts = 0
+            while sim.steps < target:
+                k = target - sim.steps
+                sim.advance(k)
+                attempts += k
+                sim.synchronize()
+            return attempts
+
+        until(warmup)
         before = sim.steps
-        total = _timed(sim._engine.stream, lambda: sim.advance(steps))
-        sim._engine.refresh()
-        done = sim.steps - before  # attempts that halved dt commit nothing
+        attempts = 0
+
+        def body():
+            nonlocal attempts
+            attempts = until(steps)
+
+        total = _timed(sim._engine.stream, body)
+        done = sim.steps - before
         ms = total / max(done, 1)
         sims[prec] = sim
         bpc = 48 if prec == "fp32" else 96
         out[prec] = {"value": n ** 3 / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
-                     "attempts": steps, "committed_steps": done, "steps": sim.steps,
+                     "attempts": attempts, "committed_steps": done, "steps": sim.steps,
                      "hbm_gbs_at_algorithmic_bytes": bpc * n ** 3 / (ms * 1e-3) / 1e9,
                      "bytes_per_cell": bpc}
-    r32, r64 = sims["fp32"].device_state[0].double(), sims["fp64"].device_state[0].double()
     out["fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
-    out["l1_rho"] = float((r32 - r64).abs().mean())
-    out["linf_rho"] = float((r32 - r64).abs().max())
+    out.update(compare_precisions(sims["fp32"], sims["fp64"], gamma))
     l32 = sims["fp32"]._engine.current_lam().double()
     l64 = sims["fp64"]._engine.current_lam().double()
     out["l1_lambda"] = float((l32 - l64).abs().mean())
-    out["fp32_balance_rel"] = float(np.max(np.abs(sims["fp32"].balance_residual))
-                                    / np.max(np.abs(sims["fp32"].initial_integral)))
+    out["linf_lambda"] = float((l32 - l64).abs().max())
+    for sim in sims.values():
+        sim.close()
+    del sims
+    torch.cuda.empty_cache()
     return out
 
 
@@ -402,19 +644,27 @@ def served_leg(rates=(10.0, 100.0, 1000.0), count=16, budget_gib=32.0, seed=0):
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference's CPU step on all host cores (its
+    Execution pool runs the HLLC batches on that many threads), on a bounded
+    slab of the headline workload, honouring --steps and --warmup.  Under
+    torchrun only rank 0 runs it."""
     if rank != 0:
         return
     cores = len(os.sched_getaffinity(0))
-    steps = max(1, min(args.steps, 5))
-    value, sample = cpu_reference(steps, min(args.warmup, 1), workers=cores)
+    value, samples, sample, kind = cpu_reference(args.steps, args.warmup, workers=cores)
+    ms = statistics.median(samples)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": N ** 3 / value * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": {"workload": "3D spherical explosion 256^3, Superbee, reflective, CFL 0.6",
-                   "sample": sample},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                   "sample": sample, "grid_timed": [N, N, 16],
+                   "ms_per_step_note": "measured per step of the 256x256x16 slab; the rate "
+                                       "is per cell, so it compares with the 256^3 GPU rate"},
+        "ms_per_step_samples": samples,
+        "ms_per_step_at_256cubed_extrapolated": N ** 3 / value * 1e3,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -431,6 +681,10 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--tile", default=None, help="tx,ty,chunk[,persistent_ctas] of the FP32 step")
     ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--accuracy-steps", type=int, default=200,
+                    help="steps of the FP32-vs-FP64 comparison of the headline workload")
+    ap.add_argument("--reactive-steps", type=int, default=300)
     ap.add_argument("--skip-reactive", action="store_true")
     ap.add_argument("--skip-metric", action="store_true")
     ap.add_argument("--metric-cells", default="128,96,96",
@@ -518,16 +772,22 @@ def main():
     sessions = [sim] + [torch_gb300.Simulation(prim, [1, 1, 1], precision="fp32", tile=tile, **kw)
                         for _ in range(max(1, args.e2e_sessions) - 1)]
     lanes = []
-    for s_i in sessions:
-        e_i = s_i._engine
-        e_i.refresh()
-        cur = e_i.current()
-        host_in = torch.empty(cur.shape, dtype=cur.dtype, pin_memory=True)
-        host_out = torch.empty_like(host_in, pin_memory=True)
-        host_in.copy_(cur)
-        lanes.append(dict(sim=s_i, eng=e_i, host_in=host_in, host_out=host_out,
-                          c=e_i.reports[0].current, down=None))
+    with near_gpu_memory(local) as placement:
+        for s_i in sessions:
+            e_i = s_i._engine
+            e_i.refresh()
+            cur = e_i.current()
+            host_in = torch.empty(cur.shape, dtype=cur.dtype, pin_memory=True)
+            host_out = torch.empty_like(host_in, pin_memory=True)
+            host_in.copy_(cur)
+            lanes.append(dict(sim=s_i, eng=e_i, host_in=host_in, host_out=host_out,
+                              c=e_i.reports[0].current, down=None))
     torch.cuda.synchronize()
+    link = link_rates(lanes[0]["host_in"], lanes[0]["eng"].current(), lanes[0]["host_out"])
+    link["gpu_numa_node"] = placement.node
+    link["host_pages_by_node"] = {str(k): v for k, v in
+                                  pages_by_node(lanes[0]["host_in"].data_ptr()).items()}
+    link["affinity_set_for_allocation"] = placement.saved is not None
     e2e_steps = max(3, min(args.steps, 10))
     main = torch.cuda.current_stream()
     up, down = torch.cuda.Stream(), torch.cuda.Stream()
@@ -564,38 +824,24 @@ def main():
     cur = eng.current()
     nbytes = cur.numel() * cur.element_size()
 
-    # FP64 plain path on the same workload (a few steps) and the FP32 error
+    # config 2 as stated: FP32 and plain FP64 advanced the full 200 steps from
+    # the same initial state, FP64 timed over them, errors of rho and p and
+    # the conservation drift of both
     extra = {}
-    if rank == 0:
-        s64 = torch_gb300.Simulation(prim, [1, 1, 1], precision="fp64", **kw)
-        s32 = torch_gb300.Simulation(prim, [1, 1, 1], precision="fp32", **kw)
-        k64 = 10
-        s64.advance(2)
-        s64.synchronize()
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        ev0.record(s64._engine.stream)
-        s64.advance(k64)
-        ev1.record(s64._engine.stream)
-        s64.synchronize()
-        ms64 = ev0.elapsed_time(ev1) / k64
-        s32.advance(2 + k64)
-        s32.synchronize()
-        r64 = s64.device_state[0].double()
-        r32 = s32.device_state[0].double()
-        p64 = s64.device_state
+    if rank == 0 and not args.skip_accuracy:
+        acc = accuracy_leg(prim, kw, n, steps=args.accuracy_steps)
         extra = {
-            "fp64_plain": {"value": cells / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64},
-            "fp32_over_fp64": (cells / (ms * 1e-3)) / (cells / (ms64 * 1e-3)),
-            "fp32_vs_fp64_after_steps": 2 + k64,
-            "l1_rho": float((r32 - r64).abs().mean()),
-            "linf_rho": float((r32 - r64).abs().max()),
-            "fp32_balance_rel": float(np.max(np.abs(s32.balance_residual))
-                                      / np.max(np.abs(s32.initial_integral))),
+            "fp64_plain": acc["fp64"],
+            "fp32_over_fp64": value / world / acc["fp64"]["value"],
+            "fp32_vs_fp64_after_steps": args.accuracy_steps,
+            "l1_rho": acc["l1_rho"], "linf_rho": acc["linf_rho"],
+            "l1_p": acc["l1_p"], "linf_p": acc["linf_p"],
+            "fp32_balance_rel": acc["fp32_balance_rel"],
+            "accuracy": acc,
         }
-        del p64
 
     if rank == 0 and not args.skip_reactive:
-        extra["reactive"] = reactive_leg()
+        extra["reactive"] = reactive_leg(steps=args.reactive_steps)
     if rank == 0 and not args.skip_metric:
         extra["metric_kernel"] = metric_leg(
             n=tuple(int(v) for v in args.metric_cells.split(",")))
@@ -606,8 +852,8 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
-        v, sample = cpu_reference(3, 1, workers=1)
-        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+        v, _, sample, kind = cpu_reference(3, 1, workers=1)
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": kind, "sample": sample}
 
     if rank == 0:
         line = {
@@ -633,6 +879,11 @@ def main():
             "e2e": {"value": world * cells / (e2e_ms * 1e-3), "unit": UNIT,
                     "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                     "ms_per_step": e2e_ms, "sessions_in_flight": len(lanes),
+                    "link": link,
+                    "copy_ceiling": {"value": world * cells / (link["floor_ms_per_session_step"]
+                                                               * 1e-3), "unit": UNIT,
+                                     "note": "one state up and one down per session-step at "
+                                             "the measured both-direction link rate"},
                     "note": "each session-step uploads its state from pinned host memory, "
                             "re-plans dt, steps and downloads the result"},
             "gpu_launches": 3 * args.steps,

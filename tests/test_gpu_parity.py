@@ -174,6 +174,60 @@ def test_session_3d_explosion_superbee_reflective_matches_oracle():
     np.testing.assert_allclose(gpu.boundary_integral[[0, 4]], 0, atol=1e-13)
 
 
+def test_session_3d_explosion_100_steps_fp64_matches_oracle():
+    """The headline scheme (3D explosion, Superbee, reflective, CFL 0.6) in
+    double precision for 100 steps at 40^3 against the oracle session.  Stated
+    criterion: relative L1 difference (sum |gpu - oracle| / sum |oracle|) per
+    conserved variable <= 1e-10, and the conservation residual at roundoff; the
+    kernels keep the reference's operation order, so the states are expected
+    to be bit-identical as well."""
+    prim = explosion_3d(40)
+    kw = dict(t_end=1.0, cfl=0.6, limiter="Superbee", boundaries=["Reflective"] * 3,
+              strict_cfl=False)
+    gpu = torch_gb300.Simulation(prim, [1, 1, 1], **kw)
+    ref = OracleSimulation(prim, [1, 1, 1], **kw)
+    for _ in range(100):
+        ref.step()
+    gpu.run(step_limit=100)
+    assert gpu.steps == ref.steps == 100
+    assert gpu.time == ref.time
+    got, want = gpu.state, ref.state
+    for k in range(5):
+        rel = np.sum(np.abs(got[k] - want[k])) / np.sum(np.abs(want[k]))
+        assert rel <= 1e-10, (k, rel)
+    np.testing.assert_array_equal(got, want)
+    assert np.max(np.abs(gpu.balance_residual) / np.abs(gpu.initial_integral).max()) < 1e-12
+
+
+def pressure(u, gamma=1.4):
+    return (gamma - 1.0) * (u[-1] - 0.5 * np.sum(u[1:-1] ** 2, axis=0) / u[0])
+
+
+def test_fp32_bulk_200_steps_rho_and_p_against_fp64():
+    """The headline workload's scheme at 128^3 for its full 200 steps: FP32
+    bulk against plain FP64 from the same initial state.  Stated tolerances:
+    L1 (mean absolute) error of density and of pressure <= 1e-5 each; the FP32
+    session's conservation residual relative to the initial integrals < 1e-6
+    (its sums and clock are FP64)."""
+    prim = explosion_3d(128)
+    kw = dict(t_end=1.0, cfl=0.6, limiter="Superbee", boundaries=["Reflective"] * 3,
+              strict_cfl=False, max_steps=10 ** 6)
+    s64 = torch_gb300.Simulation(prim, [1, 1, 1], graph_steps=10, **kw)
+    s32 = torch_gb300.Simulation(prim, [1, 1, 1], precision="fp32", graph_steps=10, **kw)
+    s64.run(step_limit=200)
+    s32.run(step_limit=200)
+    assert s64.steps == s32.steps == 200
+    u64, u32 = s64.state, s32.state
+    l1_rho = np.mean(np.abs(u32[0] - u64[0]))
+    l1_p = np.mean(np.abs(pressure(u32) - pressure(u64)))
+    assert l1_rho <= 1e-5, l1_rho
+    assert l1_p <= 1e-5, l1_p
+    assert np.all(np.isfinite(u32))
+    assert abs(s32.time - s64.time) <= 1e-5 * s64.time
+    assert np.max(np.abs(s32.balance_residual) / np.abs(s32.initial_integral).max()) < 1e-6
+    assert np.max(np.abs(s64.balance_residual) / np.abs(s64.initial_integral).max()) < 1e-12
+
+
 def test_sessions_match_reference_trajectories():
     g = load("sessions.npz")
     cases = {
