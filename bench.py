@@ -550,10 +550,54 @@ def metric_leg(n=(128, 96, 96), steps=10, warmup=2, cpu_n=(96, 64, 64), cpu_step
     return out
 
 
-def batched_leg(steps=500, count=64, seed=4, fp64_steps=20):
+def state_errors(u32, u64, gamma=1.4):
+    """L1 (mean) and L-infinity differences of density and pressure between
+    two conserved states (device tensors or arrays; any dimension)."""
+    import torch
+
+    a = torch.as_tensor(u32).double()
+    b = torch.as_tensor(u64, device=a.device).double()
+    out = {}
+    for name, x, y in (("rho", a[0], b[0]), ("p", pressure(a, gamma), pressure(b, gamma))):
+        d = (x - y).abs()
+        out["l1_" + name] = float(d.mean())
+        out["linf_" + name] = float(d.max())
+    return out
+
+
+def error_summary(rows):
+    """Largest and median of each error over a list of state_errors rows."""
+    out = {}
+    for key in ("l1_rho", "linf_rho", "l1_p", "linf_p"):
+        vals = [r[key] for r in rows]
+        out[key + "_max"] = max(vals)
+        out[key + "_median"] = statistics.median(vals)
+    return out
+
+
+def solve_alone(grid, chunk=64, graph_steps=16):
+    """Advance one grid alone until it is done or has made its maximum steps:
+    device milliseconds of the launches (CUDA events on its stream).  Steps
+    enqueued past the end are skipped by the kernels (a finished grid's tiles
+    exit at once)."""
+    from torch_gb300.batch import Batch
+
+    b = Batch([grid], graph_steps=graph_steps)
+    ms = 0.0
+    while not grid.done:
+        ms += _timed(b.stream, lambda: b.advance(chunk))
+        b.refresh()
+    b.close()
+    return ms
+
+
+def batched_leg(steps=500, count=64, seed=4):
     """64 quadrant grids (N from {64..1024}), MINBEE, FP32, `steps` steps each
     in one batch (autotuned tile, graph-captured), against the same grids
-    solved one after another alone (FP32, and the plain FP64 path)."""
+    solved one after another alone, in FP32 and in the plain FP64 path (every
+    solve measured in full); per-grid FP32-vs-FP64 errors of rho and p."""
+    import torch
+
     from torch_gb300 import autotune
     from torch_gb300.batch import Batch, Grid
 
@@ -573,6 +617,7 @@ def batched_leg(steps=500, count=64, seed=4, fp64_steps=20):
     ms = _timed(b.stream, lambda: b.advance(steps))
     b.refresh()
     done = sum(g.steps == steps for g in grids)
+    finals = [g.current.clone() for g in grids]  # FP32 results of the batch
     b.close()
     del b, grids
     seq32 = 0.0
@@ -581,62 +626,117 @@ def batched_leg(steps=500, count=64, seed=4, fp64_steps=20):
         s = Batch([g], tile=tile, graph_steps=10)
         seq32 += _timed(s.stream, lambda: s.advance(steps))
         s.close()
-    seq64 = 0.0
-    for p in prims:  # plain FP64 path alone, default tile, timed over fp64_steps
-        g = grid(p, "fp64", fp64_steps + 2)
-        s = Batch([g])
-        s.advance(2)
-        seq64 += _timed(s.stream, lambda: s.advance(fp64_steps)) * steps / fp64_steps
+    seq64, errors = 0.0, []
+    for p, u32 in zip(prims, finals):  # plain FP64 alone, every step measured
+        g = grid(p, "fp64")
+        s = Batch([g], graph_steps=10)
+        seq64 += _timed(s.stream, lambda: s.advance(steps))
+        s.refresh()
+        errors.append(state_errors(u32, g.current))
         s.close()
+    del finals
+    torch.cuda.empty_cache()
     upd = cells * steps
     return {
         "workload": f"{count} 2D quadrant Riemann grids, N in {{64..1024}} (seed {seed}), "
                     f"MINBEE, FP32, {steps} steps each, one batch",
         "grids": count, "cells": cells, "steps": steps, "grids_completed": done,
-        "tile": list(tile), "autotune_s": tune_s,
+        "tile": list(tile), "tile_source": "autotuner (torch_gb300.autotune.tune)",
+        "autotune_s": tune_s,
         "value": upd / (ms * 1e-3), "unit": UNIT, "batch_ms": ms,
-        "sequential_fp32": {"value": upd / (seq32 * 1e-3), "ms": seq32},
+        "sequential_fp32": {"value": upd / (seq32 * 1e-3), "ms": seq32,
+                            "how": "each grid alone, all its steps timed"},
         "sequential_fp64_plain": {"value": upd / (seq64 * 1e-3), "ms": seq64,
-                                  "timed_steps_per_grid": fp64_steps},
+                                  "how": "each grid alone, all its steps timed"},
         "speedup_vs_sequential_fp32": seq32 / ms,
         "speedup_vs_sequential_fp64": seq64 / ms,
+        "fp32_vs_fp64": dict(error_summary(errors),
+                             per_grid_l1_rho=[e["l1_rho"] for e in errors],
+                             per_grid_l1_p=[e["l1_p"] for e in errors],
+                             per_grid_linf_rho=[e["linf_rho"] for e in errors],
+                             per_grid_linf_p=[e["linf_p"] for e in errors]),
         "latency": "every grid finishes with the batch: p50 = p99 = batch_ms",
     }
 
 
-def served_leg(rates=(10.0, 100.0, 1000.0), count=16, budget_gib=32.0, seed=0):
+def served_leg(rates=(10.0, 30.0, 100.0, 300.0, 1000.0), count=128, budget_gib=32.0, seed=0,
+               measured_rate=100.0, fp64_budget_s=45.0):
     """Poisson request streams of the served mix (40% 1D tubes, 40% 2D, 20% 3D
     explosions at full size, t_end ~ U[0.1, 0.3]) through the continuous
-    batching server, FP32; against sequential plain FP64 solves of the same
-    requests (each request's FP64 step time alone x its step count)."""
-    from torch_gb300.batch import Batch
+    batching server, FP32, `count` requests per rate.  At `measured_rate` the
+    same requests are also solved one after another alone: all of them in
+    FP32, and in plain FP64 those that, taken in arrival order, still fit an
+    estimated `fp64_budget_s` of device time (an FP64 solve is estimated at
+    60x its FP32 time); each of those FP64 solutions
+    gives the served FP32 result's errors of rho and p, and the served result
+    is checked against the same request solved alone in FP32."""
+    import torch
+
     from torch_gb300.serve import Server, served_requests
 
     out = []
     for k, lam in enumerate(rates):
         reqs = served_requests(rate=lam, count=count, seed=seed + k)
+        measured = abs(lam - measured_rate) < 1e-9
+        seq = None
+        keep = set()
+        if measured:
+            seq32_ms, alone32, est = 0.0, {}, 0.0
+            for r in reqs:  # every request alone in FP32, measured
+                g = r.make_grid("fp32", "cuda")
+                t = solve_alone(g)
+                seq32_ms += t
+                # the leading requests whose FP64 solves fit the budget
+                # (FP64 takes about 60x the FP32 time on this GPU)
+                if est + 60 * t <= fp64_budget_s * 1e3:
+                    est += 60 * t
+                    keep.add(r.rid)
+                    alone32[r.rid] = g.current.clone()
+                del g
+            seq = {"fp32_ms": seq32_ms, "alone32": alone32}
         srv = Server(budget_bytes=int(budget_gib * (1 << 30)), precision="fp32",
-                     steps_per_tick=8)
+                     steps_per_tick=8, keep_results=keep or False)
         st = srv.run(reqs)
-        seq_ms = 0.0
-        for r in reqs:  # FP64 alone: 2 warm-up + 3 timed steps, scaled to the request's steps
-            g = r.make_grid("fp64", srv.device)
-            s = Batch([g])
-            s.advance(2)
-            seq_ms += _timed(s.stream, lambda: s.advance(3)) / 3 * max(r.steps, 1)
-            s.close()
-            del s, g
         upd = st["cell_updates"]
-        out.append({
+        entry = {
             "rate_per_s": lam, "requests": count, "completed": st["completed"],
             "p50_latency_s": st["p50_latency_s"], "p99_latency_s": st["p99_latency_s"],
             "wall_s": st["wall_s"], "cell_updates": upd,
             "value": st["cell_updates_per_s"], "unit": UNIT,
-            "sequential_fp64_plain": {"value": upd / (seq_ms * 1e-3), "s": seq_ms * 1e-3},
-            "speedup_vs_sequential_fp64": (upd / st["wall_s"]) / (upd / (seq_ms * 1e-3)),
             "mix": {d: sum(r.dim == d for r in reqs) for d in (1, 2, 3)},
             "rebuilds": srv.rebuilds,
-        })
+        }
+        if measured:
+            seq64_ms, errors, same, sub_upd = 0.0, [], 0, 0
+            for r in reqs:
+                if r.rid not in keep:
+                    continue
+                g = r.make_grid("fp64", "cuda")
+                seq64_ms += solve_alone(g)
+                served = torch.as_tensor(r.result, device="cuda")
+                alone = seq["alone32"][r.rid]
+                same += int(torch.equal(served, alone.double()))
+                e = state_errors(served, g.current)
+                e.update(rid=r.rid, dim=r.dim, n=r.n, steps=r.steps)
+                errors.append(e)
+                sub_upd += r.cells * r.steps
+                del g
+            torch.cuda.empty_cache()
+            entry["sequential_fp32"] = {
+                "value": upd / (seq["fp32_ms"] * 1e-3), "s": seq["fp32_ms"] * 1e-3,
+                "requests": count, "how": "every request alone, all its steps timed"}
+            entry["speedup_vs_sequential_fp32"] = (upd / st["wall_s"]) / (
+                upd / (seq["fp32_ms"] * 1e-3))
+            entry["sequential_fp64_plain"] = {
+                "value": sub_upd / (seq64_ms * 1e-3), "s": seq64_ms * 1e-3,
+                "requests": len(errors), "cell_updates": sub_upd,
+                "how": "requests (arrival order) whose estimated FP64 time fit the budget, "
+                       "each alone, all their steps timed"}
+            entry["speedup_vs_sequential_fp64"] = (upd / st["wall_s"]) / (
+                sub_upd / (seq64_ms * 1e-3))
+            entry["fp32_vs_fp64"] = dict(error_summary(errors), requests=errors,
+                                         served_equals_alone_fp32=f"{same}/{len(errors)}")
+        out.append(entry)
     return {"workload": "served mix: 40% 1D tubes N~logU[1e3,1e5], 40% 2D N^2 N~U[128,1024], "
                         "20% 3D N^3 N~U[64,256]; rho,p~U[0.1,2], t_end~U[0.1,0.3]; VanLeer or "
                         f"Superbee; FP32, HBM budget {budget_gib} GiB; {count} requests per rate",
@@ -692,7 +792,8 @@ def main():
     ap.add_argument("--metric-only", action="store_true",
                     help="run only the metric / face-boundary leg (--steps, --warmup) and print it")
     ap.add_argument("--skip-served", action="store_true")
-    ap.add_argument("--served-count", type=int, default=16)
+    ap.add_argument("--served-count", type=int, default=128)
+    ap.add_argument("--served-rates", default="10,30,100,300,1000")
     ap.add_argument("--e2e-sessions", type=int, default=4,
                     help="independent sessions stepped end to end on their own streams")
     ap.add_argument("--graph-steps", type=int, default=10,
@@ -848,7 +949,8 @@ def main():
     if rank == 0 and not args.skip_batched:
         extra["batched"] = batched_leg()
     if rank == 0 and not args.skip_served:
-        extra["served"] = served_leg(count=args.served_count)
+        extra["served"] = served_leg(
+            rates=tuple(float(v) for v in args.served_rates.split(",")), count=args.served_count)
 
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:

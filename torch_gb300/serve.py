@@ -133,6 +133,12 @@ class Server:
         self.ticks = 0
         self.rebuilds = 0
 
+    def _keep(self, r):
+        """keep_results: True keeps every final state on the host, a set of
+        request ids keeps those requests' states only."""
+        k = self.keep_results
+        return k is True or (bool(k) and not isinstance(k, bool) and r.rid in k)
+
     def _rebuild(self, dim):
         old = self.batches.pop(dim, None)
         if old is not None:
@@ -157,7 +163,7 @@ class Server:
                 r.finished = self.clock() - t0
                 r.steps = r.grid.steps
                 r.status = r.grid.status
-                if self.keep_results:
+                if self._keep(r):
                     r.result = r.grid.state_host()
                 self.used -= r.bytes_estimate(self.precision)
                 r.grid = None
