@@ -446,11 +446,15 @@ struct HydroTile {
 // 135-151, python/cfdSolver/torchSolver2D.py:305-377).  Writes predictor and
 // in-plane slopes to the box; returns the marching-axis slope; sets *gate when
 // a predicted face state is nonphysical (3D gate, torchSolver3D.py:152-159).
+// check_gate false skips the gate: the single-precision step gates the face
+// states of in-domain cells inside HLLC (hllc_gated), where each of them is
+// consumed, and calls this with the gate only for ghost cells, whose outer
+// face states no face consumes.
 template <typename R, int DIM, bool VARG, int LIM>
 __device__ __forceinline__ void cell_stage(const R* ringm, const R* ringc, const R* ringp,
                                            R* box, const HydroSmem<R, DIM, VARG>& S, int a,
                                            int b, R gconst, const R* coefh, R* ubar, R* smarch,
-                                           bool& gate) {
+                                           bool& gate, bool check_gate = true) {
   constexpr int NV = DIM + 2;
   const int plane = S.ph * S.pw;
   const int li = (DIM == 3 ? (b + 2) * S.pw : 0) + (a + S.xo);
@@ -527,7 +531,7 @@ __device__ __forceinline__ void cell_stage(const R* ringm, const R* ringc, const
   }
 #pragma unroll
   for (int c = 0; c < NV; ++c) bub[c * bplane + bi] = ubar[c];
-  if (DIM == 3) {
+  if (DIM == 3 && check_gate) {
     // predictor gate on every predicted face state
     bool ok = true;
 #pragma unroll
@@ -782,7 +786,11 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   const int nfa = (ax + 1) * by;
   const int nfb = DIM == 3 ? ax * (by + 1) : 0;
   int n_fitems = 0;
-  for (int w = tid; w < nfa + nfb; w += NT) {
+  // the faces do not divide evenly over the threads: the ones that take one
+  // more face than the rest start at warp 2, so that they share no warp (and
+  // no scheduler) with the ring cells of warps 0 and 1
+  const int tface = (tid + NT - 64 % NT) % NT;
+  for (int w = tface; w < nfa + nfb; w += NT) {
     int packed;
     if (w < nfa) {
       const int af = w % (ax + 1), b = w / (ax + 1);
@@ -816,7 +824,12 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
         b = (pk & 0x7fff) - 1;
       }
       R ub[NV], sm[NV];
-      cell_stage<R, DIM, VARG, LIM>(rm, rc, rp, box, S, a, b, gconst, coefh, ub, sm, gate);
+      // ghost cells (outside the domain) keep the explicit gate; the face
+      // states of in-domain cells are gated where HLLC consumes them (FP32)
+      const bool ghost = it < 0 || it >= g.np || x0 + a < 0 || x0 + a >= g.na ||
+                         (DIM == 3 && (y0 + b < 0 || y0 + b >= g.nb));
+      cell_stage<R, DIM, VARG, LIM>(rm, rc, rp, box, S, a, b, gconst, coefh, ub, sm, gate,
+                                    Exact<R>::value || ghost);
       if (k < 0) {
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
@@ -855,7 +868,10 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
           gl = rc[NV * cplane + li];
           gr = rc[NV * cplane + li + (kind == 0 ? 1 : S.pw)];
         }
-        hllc<R, NV - 3>(ul, ur, gl, gr, f);
+        if constexpr (Exact<R>::value || DIM != 3)
+          hllc<R, NV - 3>(ul, ur, gl, gr, f);
+        else
+          hllc_gated<NV - 3>(ul, ur, gl, gr, f, gate);
         R F[NV];  // back to Cartesian order
 #pragma unroll
         for (int c = 0; c < NV; ++c) F[c] = kind == 1 ? (c == 1 ? f[2] : (c == 2 ? f[1] : f[c])) : f[c];
@@ -914,7 +930,10 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
       const int li = (DIM == 3 ? (ob + 2) * S.pw : 0) + oa + S.xo;
       const R gcur = VARG ? rc[NV * cplane + li] : gconst;
       if (it >= p0) {
-        hllc_cartesian<R, NV>(Tprev, Bn, gprev, gcur, MD, Fm);
+        if constexpr (Exact<R>::value || DIM != 3)
+          hllc_cartesian<R, NV>(Tprev, Bn, gprev, gcur, MD, Fm);
+        else
+          hllc_cartesian_gated<NV>(Tprev, Bn, gprev, gcur, MD, Fm, gate);
         if (want_flux && fout[MD]) {
 #pragma unroll
           for (int c = 0; c < NV; ++c)

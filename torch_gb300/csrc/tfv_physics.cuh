@@ -302,6 +302,120 @@ __device__ __forceinline__ void normal_order(int normal, int* order) {
   order[NV - 1] = NV - 1;
 }
 
+// Single-precision HLLC of the fused step (same states, speeds and masks as
+// hllc above).  Only one physical flux is formed: the region that the masks
+// select (left, right, or the star state of the side `ss <= 0` picks, in the
+// reference's precedence: right supersonic, then star, then left
+// supersonic) reads one side's flux, so the other side's flux is never
+// needed.  It also tests both input face states for the 3D predictor gate
+// (density and internal energy density above the floor; NaN fails) and ORs
+// the result into `gate`: every predicted face state the step consumes
+// passes through here once.  NaN where no mask holds, as in hllc.
+template <int NT>
+__device__ __forceinline__ void hllc_gated(const float* ul, const float* ur, float gl, float gr,
+                                           float* out, bool& gate) {
+  constexpr int NV = NT + 3;
+  constexpr int E = NV - 1;
+  const float fl = float(kFloor);
+  const float g = 0.5f * (gl + gr);
+  const float rl = np_max(ul[0], fl);
+  const float rr = np_max(ur[0], fl);
+  const float irl = rcp(rl), irr = rcp(rr);
+  const float unl = ul[1] * irl, unr = ur[1] * irr;
+  float utl[NT], utr[NT];
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
+    utl[t] = ul[2 + t] * irl;
+    utr[t] = ur[2 + t] * irr;
+  }
+  float stl = utl[0] * utl[0], str = utr[0] * utr[0];
+#pragma unroll
+  for (int t = 1; t < NT; ++t) {
+    stl = stl + utl[t] * utl[t];
+    str = str + utr[t] * utr[t];
+  }
+  const float eil = ul[E] - (0.5f * rl) * (unl * unl + stl);  // internal energy density
+  const float eir = ur[E] - (0.5f * rr) * (unr * unr + str);
+  if (!(ul[0] > fl && eil > fl && ur[0] > fl && eir > fl)) gate = true;
+  const float pl = np_max((gl - 1.0f) * eil, fl);
+  const float pr = np_max((gr - 1.0f) * eir, fl);
+  const float al = sqrtf(gl * pl * irl);
+  const float ar = sqrtf(gr * pr * irr);
+  const float sql = sqrtf(rl), sqr = sqrtf(rr);
+  const float inv = rcp(sql + sqr);
+  const float uroe = (sql * unl + sqr * unr) * inv;
+  float vsum;
+  {
+    const float v0 = (sql * utl[0] + sqr * utr[0]) * inv;
+    vsum = v0 * v0;
+#pragma unroll
+    for (int t = 1; t < NT; ++t) {
+      const float vt = (sql * utl[t] + sqr * utr[t]) * inv;
+      vsum = vsum + vt * vt;
+    }
+  }
+  const float hl = (ul[E] + pl) * irl;
+  const float hr = (ur[E] + pr) * irr;
+  const float hroe = (sql * hl + sqr * hr) * inv;
+  const float aroe = sqrtf(np_max((g - 1.0f) * (hroe - 0.5f * (uroe * uroe + vsum)), fl));
+  const float sL = np_min(unl - al, uroe - aroe);
+  const float sR = np_max(unr + ar, uroe + aroe);
+  const float den = guarded(rl * (sL - unl) - rr * (sR - unr), float(kGuard));
+  const float ss = dv(((pr - pl) + (rl * unl) * (sL - unl)) - (rr * unr) * (sR - unr), den);
+
+  const bool mr = (0.0f >= sR);
+  const bool mstar = ((ss <= 0.0f) && (0.0f <= sR)) || ((sL <= 0.0f) && (0.0f <= ss));
+  const bool ml = (0.0f <= sL);
+  // side whose flux the selected region reads
+  const bool right = mr || (mstar && ss <= 0.0f);
+  const float rho = right ? rr : rl;
+  const float irho = right ? irr : irl;
+  const float un = right ? unr : unl;
+  const float p = right ? pr : pl;
+  const float uE = right ? ur[E] : ul[E];
+  float u[NV], f[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) u[c] = right ? ur[c] : ul[c];
+  const float mn = rho * un;
+  f[0] = mn;
+  f[1] = mn * un + p;
+#pragma unroll
+  for (int t = 0; t < NT; ++t) f[2 + t] = mn * (right ? utr[t] : utl[t]);
+  f[E] = un * (uE + p);
+  const float s = right ? sR : sL;
+  if (!mr && mstar && !(fabsf(s - ss) < fl)) {
+    const float rho_s = np_max(rho * dv(s - un, guarded(s - ss, float(kGuard))), fl);
+    const float dun = guarded(s - un, float(kGuard));
+    float star[NV];
+    star[0] = rho_s;
+    star[1] = rho_s * ss;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) star[2 + t] = rho_s * (right ? utr[t] : utl[t]);
+    star[E] = rho_s * (uE * irho + (ss - un) * (ss + dv(p, rho * dun)));
+#pragma unroll
+    for (int c = 0; c < NV; ++c) f[c] = f[c] + s * (star[c] - u[c]);
+  }
+  const bool any = mr || mstar || ml;
+#pragma unroll
+  for (int c = 0; c < NV; ++c) out[c] = any ? f[c] : NAN;
+}
+
+template <int NV>
+__device__ __forceinline__ void hllc_cartesian_gated(const float* L, const float* Rt, float gl,
+                                                     float gr, int d, float* F, bool& gate) {
+  int order[NV];
+  normal_order<NV>(d + 1, order);
+  float ul[NV], ur[NV], f[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) {
+    ul[c] = L[order[c]];
+    ur[c] = Rt[order[c]];
+  }
+  hllc_gated<NV - 3>(ul, ur, gl, gr, f, gate);
+#pragma unroll
+  for (int c = 0; c < NV; ++c) F[order[c]] = f[c];
+}
+
 // HLLC across a face along direction d (0=x,1=y,2=z) with Cartesian inputs
 // and output (python/cfdSolver/torchFlux.py:6-77 without the batching).
 template <typename R, int NV>
