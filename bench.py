@@ -137,7 +137,8 @@ def reference_modules():
     pkg = types.ModuleType("cfdSolver")
     pkg.__path__ = [base]
     sys.modules["cfdSolver"] = pkg
-    return types.SimpleNamespace(session=importlib.import_module("cfdSolver.torchSession"))
+    return types.SimpleNamespace(session=importlib.import_module("cfdSolver.torchSession"),
+                                 adaptive=importlib.import_module("cfdSolver.torchAdaptive"))
 
 
 def cpu_reference(steps, warmup, nz=16, workers=1):
@@ -353,14 +354,20 @@ def compare_precisions(s32, s64, gamma):
         out["l1_" + name] = float(d.mean())
         out["linf_" + name] = float(d.max())
         out["rel_l1_" + name] = float(d.sum() / b.abs().sum())
-    scale = lambda s: np.maximum(np.abs(s.initial_integral), 1e-300)
+    def scale(s):
+        # per-variable scale: the variable's initial integral, or the largest
+        # initial integral for variables that start at zero (the momenta)
+        i0 = np.abs(s.initial_integral)
+        return np.where(i0 > 1e-12 * i0.max(), i0, i0.max())
+
     for tag, s in (("fp32", s32), ("fp64", s64)):
         out[tag + "_balance_rel"] = float(np.max(np.abs(s.balance_residual)
                                                  / np.maximum(np.abs(s.initial_integral), 1.0)))
         out[tag + "_balance_rel_per_var"] = (np.abs(s.balance_residual) / scale(s)).tolist()
     i32, i64 = s32.integral, s64.integral
-    out["fp32_integral_rel_to_fp64"] = (np.abs(i32 - i64)
-                                        / np.maximum(np.abs(i64), 1e-300)).tolist()
+    out["fp32_integral_rel_to_fp64"] = (np.abs(i32 - i64) / scale(s64)).tolist()
+    out["per_var_note"] = ("rho, momenta, E; relative to each variable's initial integral, "
+                           "or to the largest one where a variable starts at zero")
     out["time_fp32"], out["time_fp64"] = s32.time, s64.time
     out["steps_fp32"], out["steps_fp64"] = s32.steps, s64.steps
     return out
@@ -660,16 +667,17 @@ def batched_leg(steps=500, count=64, seed=4):
 
 
 def served_leg(rates=(10.0, 30.0, 100.0, 300.0, 1000.0), count=128, budget_gib=32.0, seed=0,
-               measured_rate=100.0, fp64_budget_s=45.0):
+               measured_rate=100.0, fp64_budget_s=45.0, check=8):
     """Poisson request streams of the served mix (40% 1D tubes, 40% 2D, 20% 3D
     explosions at full size, t_end ~ U[0.1, 0.3]) through the continuous
     batching server, FP32, `count` requests per rate.  At `measured_rate` the
     same requests are also solved one after another alone: all of them in
-    FP32, and in plain FP64 those that, taken in arrival order, still fit an
-    estimated `fp64_budget_s` of device time (an FP64 solve is estimated at
-    60x its FP32 time); each of those FP64 solutions
-    gives the served FP32 result's errors of rho and p, and the served result
-    is checked against the same request solved alone in FP32."""
+    FP32, and in plain FP64 those that, taken in arrival order, fit
+    `fp64_budget_s` of device time (each FP64 solve is estimated from its FP32
+    time and the FP64/FP32 ratio measured so far).  Each FP64 solution gives
+    the errors of rho and p of that request's FP32 result; the first `check`
+    served results are compared bit for bit with the same requests solved
+    alone in FP32."""
     import torch
 
     from torch_gb300.serve import Server, served_requests
@@ -678,24 +686,9 @@ def served_leg(rates=(10.0, 30.0, 100.0, 300.0, 1000.0), count=128, budget_gib=3
     for k, lam in enumerate(rates):
         reqs = served_requests(rate=lam, count=count, seed=seed + k)
         measured = abs(lam - measured_rate) < 1e-9
-        seq = None
-        keep = set()
-        if measured:
-            seq32_ms, alone32, est = 0.0, {}, 0.0
-            for r in reqs:  # every request alone in FP32, measured
-                g = r.make_grid("fp32", "cuda")
-                t = solve_alone(g)
-                seq32_ms += t
-                # the leading requests whose FP64 solves fit the budget
-                # (FP64 takes about 60x the FP32 time on this GPU)
-                if est + 60 * t <= fp64_budget_s * 1e3:
-                    est += 60 * t
-                    keep.add(r.rid)
-                    alone32[r.rid] = g.current.clone()
-                del g
-            seq = {"fp32_ms": seq32_ms, "alone32": alone32}
+        keep = {r.rid for r in reqs[:check]} if measured else False
         srv = Server(budget_bytes=int(budget_gib * (1 << 30)), precision="fp32",
-                     steps_per_tick=8, keep_results=keep or False)
+                     steps_per_tick=8, keep_results=keep)
         st = srv.run(reqs)
         upd = st["cell_updates"]
         entry = {
@@ -707,40 +700,109 @@ def served_leg(rates=(10.0, 30.0, 100.0, 300.0, 1000.0), count=128, budget_gib=3
             "rebuilds": srv.rebuilds,
         }
         if measured:
-            seq64_ms, errors, same, sub_upd = 0.0, [], 0, 0
-            for r in reqs:
-                if r.rid not in keep:
+            seq32_ms, t32, alone32, same = 0.0, {}, {}, 0
+            for r in reqs:  # every request alone in FP32, measured
+                g = r.make_grid("fp32", "cuda")
+                t32[r.rid] = solve_alone(g)
+                seq32_ms += t32[r.rid]
+                alone32[r.rid] = g.current.clone()
+                if r.rid in keep:
+                    same += int(torch.equal(torch.as_tensor(r.result, device="cuda"),
+                                            alone32[r.rid].double()))
+                del g
+            seq64_ms, sub32_ms, errors, sub_upd = 0.0, 0.0, [], 0
+            for r in reqs:  # FP64 alone, arrival order, within the budget
+                ratio = seq64_ms / sub32_ms if sub32_ms > 0 else 60.0
+                if seq64_ms + ratio * t32[r.rid] > fp64_budget_s * 1e3:
                     continue
                 g = r.make_grid("fp64", "cuda")
                 seq64_ms += solve_alone(g)
-                served = torch.as_tensor(r.result, device="cuda")
-                alone = seq["alone32"][r.rid]
-                same += int(torch.equal(served, alone.double()))
-                e = state_errors(served, g.current)
+                sub32_ms += t32[r.rid]
+                e = state_errors(alone32[r.rid], g.current)
                 e.update(rid=r.rid, dim=r.dim, n=r.n, steps=r.steps)
                 errors.append(e)
                 sub_upd += r.cells * r.steps
                 del g
+            del alone32
             torch.cuda.empty_cache()
             entry["sequential_fp32"] = {
-                "value": upd / (seq["fp32_ms"] * 1e-3), "s": seq["fp32_ms"] * 1e-3,
+                "value": upd / (seq32_ms * 1e-3), "s": seq32_ms * 1e-3,
                 "requests": count, "how": "every request alone, all its steps timed"}
-            entry["speedup_vs_sequential_fp32"] = (upd / st["wall_s"]) / (
-                upd / (seq["fp32_ms"] * 1e-3))
+            entry["speedup_vs_sequential_fp32"] = (upd / st["wall_s"]) / (upd / (seq32_ms * 1e-3))
             entry["sequential_fp64_plain"] = {
                 "value": sub_upd / (seq64_ms * 1e-3), "s": seq64_ms * 1e-3,
                 "requests": len(errors), "cell_updates": sub_upd,
+                "mix": {d: sum(e["dim"] == d for e in errors) for d in (1, 2, 3)},
                 "how": "requests (arrival order) whose estimated FP64 time fit the budget, "
                        "each alone, all their steps timed"}
             entry["speedup_vs_sequential_fp64"] = (upd / st["wall_s"]) / (
                 sub_upd / (seq64_ms * 1e-3))
             entry["fp32_vs_fp64"] = dict(error_summary(errors), requests=errors,
-                                         served_equals_alone_fp32=f"{same}/{len(errors)}")
+                                         served_equals_alone_fp32=f"{same}/{len(keep)}")
         out.append(entry)
     return {"workload": "served mix: 40% 1D tubes N~logU[1e3,1e5], 40% 2D N^2 N~U[128,1024], "
                         "20% 3D N^3 N~U[64,256]; rho,p~U[0.1,2], t_end~U[0.1,0.3]; VanLeer or "
                         f"Superbee; FP32, HBM budget {budget_gib} GiB; {count} requests per rate",
             "sweep": out}
+
+
+def adaptive_leg(n=64, steps=6, warmup=1):
+    """The reference's adaptive session (AdaptiveSimulation, 2D explosion on an
+    n^2 root grid, two refinement levels) stepped with its own CPU leaf-face
+    Rusanov batches and with the batches on the GPU (torch_gb300.adaptive):
+    whole-step times and the time spent in the flux batches, and the final
+    states compared.  The mesh, face reconstruction and accumulation stay on
+    the host in both runs, as in the reference."""
+    R = reference_modules()
+    if R is None:
+        return {"unavailable": "the reference is not installed in baseline/_ref"}
+    from torch_gb300 import adaptive as gpu_adaptive
+
+    c = (np.arange(n) + 0.5) / n
+    Y, X = np.meshgrid(c, c, indexing="ij")
+    inside = (X - 0.5) ** 2 + (Y - 0.5) ** 2 <= 0.2 ** 2
+    p = np.zeros((4, n, n))
+    p[0] = np.where(inside, 1.0, 0.125)
+    p[3] = np.where(inside, 1.0, 0.1)
+    out = {"workload": f"reference AdaptiveSimulation, 2D explosion, {n}^2 root grid, "
+                       f"max_level 2, {steps} steps after {warmup}"}
+    finals = {}
+    for kind in ("cpu", "gpu"):
+        a = R.session.Simulation(p, [1.0, 1.0], t_end=1.0).to_adaptive(max_level=2)
+        flux_s = [0.0]
+        faces = [0]
+        inner = R.adaptive.rusanov if kind == "cpu" else None
+
+        def timed_flux(left, right, gl, gr, k, inner=inner):
+            t0 = time.perf_counter()
+            v = (inner(left, right, gl, gr, k) if inner is not None
+                 else gpu_adaptive.leaf_fluxes(left, right, gl, gr, k))
+            flux_s[0] += time.perf_counter() - t0
+            faces[0] += left.shape[1]
+            return v
+
+        original = R.adaptive.rusanov
+        R.adaptive.rusanov = timed_flux
+        try:
+            for _ in range(warmup):
+                a.step()
+            flux_s[0], faces[0] = 0.0, 0
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                a.step()
+            wall = time.perf_counter() - t0
+        finally:
+            R.adaptive.rusanov = original
+        leaves = len(a.mesh.keys)
+        out[kind] = {"ms_per_step": wall * 1e3 / steps, "flux_ms_per_step": flux_s[0] * 1e3 / steps,
+                     "faces_per_step": faces[0] / steps, "leaves": leaves,
+                     "leaf_updates_per_s": leaves * steps / wall}
+        finals[kind] = a.state
+    out["flux_speedup"] = out["cpu"]["flux_ms_per_step"] / out["gpu"]["flux_ms_per_step"]
+    out["step_speedup"] = out["cpu"]["ms_per_step"] / out["gpu"]["ms_per_step"]
+    out["gpu_equals_cpu_bitwise"] = bool(finals["cpu"].shape == finals["gpu"].shape
+                                         and np.array_equal(finals["cpu"], finals["gpu"]))
+    return out
 
 
 def run_reference(args, rank, world):
@@ -782,6 +844,7 @@ def main():
     ap.add_argument("--tile", default=None, help="tx,ty,chunk[,persistent_ctas] of the FP32 step")
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--skip-adaptive", action="store_true")
     ap.add_argument("--accuracy-steps", type=int, default=200,
                     help="steps of the FP32-vs-FP64 comparison of the headline workload")
     ap.add_argument("--reactive-steps", type=int, default=300)
@@ -946,6 +1009,8 @@ def main():
     if rank == 0 and not args.skip_metric:
         extra["metric_kernel"] = metric_leg(
             n=tuple(int(v) for v in args.metric_cells.split(",")))
+    if rank == 0 and not args.skip_adaptive:
+        extra["adaptive"] = adaptive_leg()
     if rank == 0 and not args.skip_batched:
         extra["batched"] = batched_leg()
     if rank == 0 and not args.skip_served:
