@@ -4,7 +4,7 @@ Run where the reference source tree is available, naming its root (the
 directory that holds ``python/cfdSolver``) with ``--reference`` or
 ``$TORCH_REFERENCE``:
 
-    python tests/golden/make_golden.py --reference PATH [checkpoint|metric|rusanov|output]
+    python tests/golden/make_golden.py --reference PATH [checkpoint|metric|rusanov|output|adaptive]
 
 The reference package ``cfdSolver`` imports matplotlib at package level, so it
 is loaded through a bare namespace module whose ``__path__`` points at the
@@ -545,6 +545,51 @@ def rusanov_cases(R):
     np.savez_compressed(OUT / "rusanov.npz", **out)
 
 
+def adaptive_sessions(S):
+    """The two adaptive sessions of the adaptive trajectories (also built by
+    tests/test_gpu_adaptive.py): a 2D Cartesian explosion on a 32^2 root grid
+    with two refinement levels, and the refined 2D cylindrical blast of the
+    leaf-face batches above."""
+    n = 32
+    c = (np.arange(n) + 0.5) / n
+    Y, X = np.meshgrid(c, c, indexing="ij")
+    inside = (X - 0.5) ** 2 + (Y - 0.5) ** 2 <= 0.2 ** 2
+    p = np.zeros((4, n, n))
+    p[0] = np.where(inside, 1.0, 0.125)
+    p[3] = np.where(inside, 1.0, 0.1)
+    explosion = S(p, [1.0, 1.0], t_end=0.2).to_adaptive(max_level=2)
+    counts = [12, 8]
+    q = np.ones((4, *counts[::-1]))
+    q[1:-1] = 0.0
+    r = 0.2 + (np.arange(counts[0]) + 0.5) / counts[0]
+    q[-1] = np.where(r < 0.5, 4.0, 1.0)[None, :]
+    s = S(q, [1.0, 1.0], geometry="cylindrical", origins=[0.2, 0.0], t_end=0.05)
+    blast = s.to_adaptive(max_level=2)
+    blast.regrid(refine=blast.mesh.centers[:, 0] < 0.7, coarsen=False)
+    return {"explosion2d": (explosion, 8), "cylindrical_blast": (blast, 4)}
+
+
+def adaptive_cases(R):
+    """Trajectories of the reference's AdaptiveSimulation (torchAdaptive.py:
+    346-492) with its own CPU Rusanov fluxes: every step's time, leaf count
+    and boundary integral, and the final leaf keys and state."""
+    out = {}
+    for name, (a, steps) in adaptive_sessions(R.torchSession.Simulation).items():
+        times, leaves, bnd = [], [], []
+        for _ in range(steps):
+            a.step()
+            times.append(a.time)
+            leaves.append(len(a.mesh.keys))
+            bnd.append(a.boundary_integral.copy())
+        out[f"{name}|time"] = np.array(times)
+        out[f"{name}|leaves"] = np.array(leaves)
+        out[f"{name}|boundary"] = np.array(bnd)
+        out[f"{name}|keys"] = np.array(a.mesh.keys)
+        out[f"{name}|state"] = a.state
+        out[f"{name}|steps"] = np.array([a.steps])
+    np.savez_compressed(OUT / "adaptive.npz", **out)
+
+
 def output_cases(R):
     """The reference's field output (torchIO.py:122-733): VTK rectilinear and
     structured snapshots, XDMF snapshots with their HDF5 heavy data, and the
@@ -688,7 +733,8 @@ def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--reference", default=os.environ.get("TORCH_REFERENCE"),
                     help="root of the TORCH source tree (default: $TORCH_REFERENCE)")
-    ap.add_argument("case", nargs="?", choices=["checkpoint", "metric", "rusanov", "output"],
+    ap.add_argument("case", nargs="?",
+                    choices=["checkpoint", "metric", "rusanov", "output", "adaptive"],
                     help="regenerate this fixture alone")
     args = ap.parse_args()
     if not args.reference:
@@ -698,7 +744,8 @@ def main():
         ap.error(f"{REF / 'cfdSolver'} is not a directory")
     R = load_reference()
     single = {"checkpoint": checkpoint_cases, "metric": metric_cases,
-              "rusanov": rusanov_cases, "output": output_cases}
+              "rusanov": rusanov_cases, "output": output_cases,
+              "adaptive": adaptive_cases}
     if args.case:
         single[args.case](R)
         return
@@ -714,6 +761,7 @@ def main():
     metric_cases(R)
     rusanov_cases(R)
     output_cases(R)
+    adaptive_cases(R)
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -121,8 +121,9 @@ def rusanov_flux(left, right, gl, gr, direction, precision="fp64"):
                                     nv, m, int(direction), _lib.ptr(lt), _lib.ptr(rt),
                                     _lib.ptr(g_l), _lib.ptr(g_r), _lib.ptr(out),
                                     _lib.stream_ptr(stream)))
-    stream.synchronize()
     out = out.reshape(shape)
+    # device inputs: the result stays on the device, ordered on the current
+    # stream (no host round trip); host inputs: copied back
     return _out(out.to(torch.float64) if host else out, host)
 
 
