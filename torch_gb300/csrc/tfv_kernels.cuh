@@ -29,10 +29,6 @@
 #include "tfv_physics.cuh"
 #include "tfv_types.h"
 
-#ifndef TFV_OWNER_FACES
-#define TFV_OWNER_FACES 1
-#endif
-
 namespace tfv {
 
 enum : int { kBcOpen = 0, kBcReflective = 1, kBcPeriodic = 2, kBcInflow = 3 };
@@ -319,25 +315,16 @@ struct HydroSmem {
   // x offset of cell a = 0 in a staged row: a tensor-copy box must start on a
   // 16-byte boundary, so the row holds 16 bytes of halo on each side.
   static constexpr int kXo = 16 / (int)sizeof(R);
-  // Owner-face layout of 16 x 16 single-precision 3D tiles (hydro_tile16):
-  // the box rows are 24 values apart, so that the two half-warps of a warp
-  // (rows b and b + 2) touch disjoint banks; the in-plane fluxes are kept in
-  // thread order, each owner storing its own left x face and bottom y face,
-  // with the far-edge faces of the tile at bank-chosen slots behind them.
-  static constexpr int kFaStride = 512;  // x faces: 256 owners + far edge at fa_edge(b)
-  static constexpr int kFbStride = 272;  // y faces: 256 owners + far edge at 256 + a
   int tx, ty, pw, ph, bw, bh, xo;
-  bool owner_faces;
   size_t slot_elems;  // elements per ring slot (128-byte multiple)
   size_t ring_off, bar_off, box_off, fa_off, fb_off, bs_off, red_off, items_off, bytes;
-  __host__ __device__ void init(int tx_, int ty_, bool owner_faces_ = false) {
+  __host__ __device__ void init(int tx_, int ty_) {
     tx = tx_;
     ty = DIM == 3 ? ty_ : 1;
-    owner_faces = owner_faces_;
     xo = kXo;
     pw = tx + 2 * kXo;
     ph = DIM == 3 ? ty + 4 : 1;
-    bw = owner_faces ? 24 : tx + 2;
+    bw = tx + 2;
     bh = DIM == 3 ? ty + 2 : 1;
     slot_elems = ((size_t)NL * ph * pw * sizeof(R) + 127) / 128 * 128 / sizeof(R);
     size_t o = 0;
@@ -350,17 +337,17 @@ struct HydroSmem {
     o += sizeof(R) * (DIM == 3 ? 3 : 2) * NV * bh * bw;
     o = (o + 15) & ~size_t(15);
     fa_off = o;
-    o += sizeof(R) * NV * (owner_faces ? kFaStride : ty * (tx + 1));
+    o += sizeof(R) * NV * ty * (tx + 1);
     o = (o + 15) & ~size_t(15);
     fb_off = o;
-    if (DIM == 3) o += sizeof(R) * NV * (owner_faces ? kFbStride : (ty + 1) * tx);
+    if (DIM == 3) o += sizeof(R) * NV * (ty + 1) * tx;
     o = (o + 15) & ~size_t(15);
     bs_off = o;  // boundary-face accumulators (double)
     o += sizeof(double) * (2 * ty * NV + (DIM == 3 ? 2 * tx * NV : 0) + 2 * NV);
     red_off = o;  // reduction scratch
     o += sizeof(double) * 40;
     items_off = o;  // per-thread ring and face work items, packed
-    if (!owner_faces) o += sizeof(int) * (kMaxRingItems + kMaxFaceItems) * tx * ty;
+    o += sizeof(int) * (kMaxRingItems + kMaxFaceItems) * tx * ty;
     bytes = ((o + 15) & ~size_t(15)) + 128;  // + room to align the base to 128 bytes
   }
 };
@@ -1022,359 +1009,6 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   return true;
 }
 
-// --------------------------------------------------------------------------
-// hydro_tile16: the fused step for 16 x 16 single-precision 3D tiles with
-// every shared-memory access of the interior cells free of bank conflicts.
-// Same arithmetic as hydro_tile, different work assignment:
-//  * owner (a, b) of thread tid: warp w holds rows r0 = 4 (w / 2) + w % 2 and
-//    r0 + 2 (one per half-warp), lanes along a.  The staged rows are 24
-//    values apart, so the half-warps' rows (48 apart) use disjoint banks.
-//  * each owner evaluates its own left x face and bottom y face and stores
-//    the fluxes in thread order; warp 2 evaluates the tile's far-edge faces
-//    (x face at a = ax, y face at b = by); warps 0 and 1 take the ring cells.
-//  * the update reads the right face from the owner of (a + 1, b) (the next
-//    lane) and the top face from the owner of (a, b + 1) (lanes of the
-//    neighbouring warp in the same bank order).
-// --------------------------------------------------------------------------
-// Tile shapes that run hydro_tile16 (and its shared-memory layout).
-template <typename R, int DIM, bool VARG, int TX, int TY>
-struct OwnerFaces {
-  static constexpr bool value =
-      !Exact<R>::value && DIM == 3 && !VARG && TX == 16 && TY == 16 && TFV_OWNER_FACES;
-};
-
-__device__ __forceinline__ int owner16_tid(int a, int b) {
-  return 32 * (2 * (b >> 2) + (b & 1)) + 16 * ((b >> 1) & 1) + a;
-}
-// slot of the far-edge x face of row b: the lanes of a = 15 in a warp (rows
-// b, b + 2) read banks 0 and 16, which no other lane of the warp reads
-__device__ __forceinline__ int fa_edge16(int b) {
-  return 256 + 64 * (b >> 2) + 32 * (b & 1) + 16 * ((b >> 1) & 1);
-}
-
-template <int LIM>
-__device__ bool hydro_tile16(const StepArgs& A, int t, unsigned char* smem,
-                             const HydroSmem<float, 3, false>& S, uint32_t& bar_phase) {
-  using R = float;
-  constexpr int DIM = 3, NV = 5, MD = 2;
-  constexpr bool VARG = false;
-  constexpr int FA = HydroSmem<R, DIM, VARG>::kFaStride;
-  constexpr int FB = HydroSmem<R, DIM, VARG>::kFbStride;
-  if (!TFV_IN(10, t, A.ntiles)) return true;
-  const Tile T = A.tiles[t];
-  if (!TFV_IN(11, T.inst, A.ninst)) return true;
-  const InstDesc& d = A.desc[T.inst];
-  InstState& st = A.st[T.inst];
-  if (st.status != kReady) return true;  // uniform over the CTA
-  Geo<DIM> g;
-  g.init(d);
-  const int src = (st.cur + A.src_off) % d.nring;
-  const int dst = (st.cur + A.dst_off) % d.nring;
-  const R* U = (const R*)d.U[src];
-  R* Un = (R*)d.U[dst];
-  const R gconst = desc_gamma(d, R(0));
-  R coefh[DIM], cu[DIM];
-#pragma unroll
-  for (int k = 0; k < DIM; ++k) {
-    coefh[k] = R(st.coef_half[k]);
-    cu[k] = R(st.coef_full[k]);
-  }
-  const int x0 = T.x0, y0 = T.y0, p0 = T.p0, p1 = T.p1;
-  const int ax = min(16, g.na - x0);
-  const int by = min(16, g.nb - y0);
-  if (!TFV_IN(12, ax - 1, 16) || !TFV_IN(13, by - 1, 16) || !TFV_IN(14, p0, p1) ||
-      !TFV_IN(15, p1 - 1, g.np) || !TFV_IN(16, blockDim.x - 1, 256) ||
-      !TFV_IN(17, (int)src, d.nring) || !TFV_IN(18, (int)dst, d.nring))
-    return true;
-  const int tid = threadIdx.x;
-  const int warp = tid >> 5, lane = tid & 31;
-  const int oa = lane & 15;
-  const int ob = 4 * (warp >> 1) + (warp & 1) + 2 * (lane >> 4);
-  const bool owner = oa < ax && ob < by;
-  const bool at_x0 = (x0 == 0), at_x1 = (x0 + ax == g.na);
-  const bool at_y0 = y0 == 0, at_y1 = (y0 + by == g.nb);
-
-  const int plane = (int)S.slot_elems;
-  const int cplane = S.ph * S.pw;
-  const int bplane = S.bh * S.bw;
-  R* ring = smem_at<R>(smem, S.ring_off);
-  R* box = smem_at<R>(smem, S.box_off);
-  R* fa = smem_at<R>(smem, S.fa_off);
-  R* fb = smem_at<R>(smem, S.fb_off);
-  double* bs = smem_at<double>(smem, S.bs_off);
-  double* red = smem_at<double>(smem, S.red_off);
-  const int nbs = 2 * 16 * NV + 2 * 16 * NV + 2 * NV;
-  for (int e = tid; e < nbs; e += blockDim.x) bs[e] = 0.0;
-  double* bs_a = bs;                 // [2][16][NV]
-  double* bs_b = bs + 2 * 16 * NV;   // [2][16][NV]
-  double* bs_m = bs_b + 2 * 16 * NV; // [2][NV]
-
-  auto slot_of = [&](int p) { return (p - p0 + 2) % 3; };
-  auto slot = [&](int p) { return ring + slot_of(p) * plane; };
-  const bool use_tma = d.tma != 0;
-  const bool edge_tile = x0 == 0 || x0 + ax + 2 > g.na || y0 == 0 || y0 + by + 2 > g.nb;
-  const char* maps = reinterpret_cast<const char*>(A.tmaps) + (size_t)T.inst * 4 * 128;
-  const void* map_u = maps + src * 128;
-  const uint32_t box_bytes = (uint32_t)(sizeof(R) * NV * S.ph * S.pw);
-  uint64_t* bars = smem_at<uint64_t>(smem, S.bar_off);
-  bool waited_ok = true;
-  if (use_tma && tid == 0) fence_tensormap_acquire(map_u);
-  auto stage_begin = [&](int p) {
-    R* dstp = slot(p);
-    if (use_tma && p >= 0 && p < g.np) {
-      if (tid == 0) {
-        uint64_t* bar = bars + slot_of(p);
-        fence_proxy_async();
-        mbar_expect_tx(bar, box_bytes);
-        tma_load_4d(dstp, map_u, x0 - S.xo, y0 - 2, p, 0, bar);
-      }
-    } else {
-      HydroTile<R, DIM, VARG>::load_plane(d, g, U, nullptr, dstp, S, x0, y0, ax, by, p);
-    }
-  };
-  auto stage_end = [&](int p) {
-    if (use_tma && p >= 0 && p < g.np) {
-      const int sidx = slot_of(p);
-      const uint32_t parity = (bar_phase >> sidx) & 1u;
-      bar_phase ^= 1u << sidx;
-      if (!mbar_wait(bars + sidx, parity)) {
-        waited_ok = false;
-        mbar_wait(bars + sidx, parity);
-      }
-      if (edge_tile)
-        HydroTile<R, DIM, VARG>::fix_ghosts(d, g, U, nullptr, slot(p), S, x0, y0, ax, by, p);
-    }
-  };
-  stage_begin(p0 - 2);
-  stage_begin(p0 - 1);
-  stage_begin(p0);
-  stage_end(p0 - 2);
-  stage_end(p0 - 1);
-  stage_end(p0);
-  if (__syncthreads_or(!waited_ok)) {
-    if (tid == 0) st.status = kErrDeviceWait;
-    return false;
-  }
-
-  R Tprev[NV], Fprev[NV], Pprev[NV];
-#pragma unroll
-  for (int c = 0; c < NV; ++c) Tprev[c] = Fprev[c] = Pprev[c] = R(0);
-  R wmax[DIM];
-#pragma unroll
-  for (int k = 0; k < DIM; ++k) wmax[k] = R(0);
-  bool bad = false, gate = false;
-  R* fout[3] = {(R*)d.flux_out[0], (R*)d.flux_out[1], (R*)d.flux_out[2]};
-  const bool want_flux = d.has_flux_out != 0;
-  const int nvo = d.flux_nv;
-
-  // ring cell (or domain corner) of this thread, if any (recomputed per
-  // plane: cheaper than keeping it in registers): warps 0 and 1 take the
-  // 2 ax + 2 by ring cells, lanes 0..3 of warp 2 the domain corners
-  auto ring_cell = [&](int& a, int& b) -> bool {
-    const int q = tid;
-    if (q < 2 * ax + 2 * by) {
-      if (q < by) { a = -1; b = q; }
-      else if (q < 2 * by) { a = ax; b = q - by; }
-      else if (q < 2 * by + ax) { a = q - 2 * by; b = -1; }
-      else { a = q - 2 * by - ax; b = by; }
-      return true;
-    }
-    const int k = q - 64;  // corners in the order x0y0, x1y0, x0y1, x1y1
-    if (k < 0 || k >= 4) return false;
-    const bool cx1 = k & 1, cy1 = k & 2;
-    if (!((cx1 ? at_x1 : at_x0) && (cy1 ? at_y1 : at_y0))) return false;
-    a = cx1 ? ax : -1;
-    b = cy1 ? by : -1;
-    return true;
-  };
-  // far-edge face of warp 2: lanes 0..15 the x face (a = ax) of row lane,
-  // lanes 16..31 the y face (b = by) of column lane - 16
-  const bool edge_x = warp == 2 && lane < 16 && lane < by;
-  const bool edge_y = warp == 2 && lane >= 16 && lane - 16 < ax;
-
-  for (int it = p0 - 1; it <= p1; ++it) {
-    const R* rm = slot(it - 1);
-    const R* rc = slot(it);
-    const R* rp = slot(it + 1);
-    const bool full = (it >= p0 && it < p1);
-    const bool edge_plane = (it == -1 || it == g.np);
-    const bool ring_now = tid < 68 && (full || edge_plane);
-    R Bn[NV], Tn[NV];
-#pragma unroll
-    for (int c = 0; c < NV; ++c) Bn[c] = Tn[c] = R(0);
-    for (int k = owner ? -1 : 0; k < (ring_now ? 1 : 0); ++k) {
-      int a = oa, b = ob;
-      if (k >= 0 && !ring_cell(a, b)) break;
-      const bool ghost = it < 0 || it >= g.np || x0 + a < 0 || x0 + a >= g.na ||
-                         y0 + b < 0 || y0 + b >= g.nb;
-      R ub[NV], sm[NV];
-      cell_stage<R, DIM, VARG, LIM>(rm, rc, rp, box, S, a, b, gconst, coefh, ub, sm, gate, ghost);
-      if (k < 0) {
-#pragma unroll
-        for (int c = 0; c < NV; ++c) {
-          Bn[c] = ub[c] - R(0.5) * sm[c];
-          Tn[c] = ub[c] + R(0.5) * sm[c];
-        }
-      }
-    }
-    __syncthreads();  // box complete; ring slot of plane it-1 free
-    const bool stage_next = it + 2 <= p1 + 1;
-    if (stage_next) stage_begin(it + 2);
-    if (full) {
-      // kind 0: x face at (i, j) between cells (i-1, j) and (i, j);
-      // kind 1: y face at (i, j) between cells (i, j-1) and (i, j)
-      for (int k = 0; k < 3; ++k) {
-        int kind, i, j, slot_f;
-        if (k < 2) {
-          if (!owner) continue;
-          kind = k;
-          i = oa;
-          j = ob;
-          slot_f = tid;
-        } else if (edge_x) {
-          kind = 0;
-          i = ax;
-          j = lane;
-          slot_f = fa_edge16(lane);
-        } else if (edge_y) {
-          kind = 1;
-          i = lane - 16;
-          j = by;
-          slot_f = 256 + (lane - 16);
-        } else {
-          continue;
-        }
-        const int br = (j + 1) * S.bw + (i + 1);  // box index of cell (i, j)
-        const int bl = br - (kind == 0 ? 1 : S.bw);
-        if (!TFV_IN(21, bl, bplane) || !TFV_IN(22, br, bplane)) continue;
-        const R* bsl = box + (kind == 0 ? 1 : 2) * NV * bplane;
-        R ul[NV], ur[NV], f[NV];
-#pragma unroll
-        for (int c = 0; c < NV; ++c) {
-          const int cc = (kind == 1 && c == 1) ? 2 : ((kind == 1 && c == 2) ? 1 : c);
-          ul[c] = box[cc * bplane + bl] + R(0.5) * bsl[cc * bplane + bl];
-          ur[c] = box[cc * bplane + br] - R(0.5) * bsl[cc * bplane + br];
-        }
-        hllc_gated<NV - 3>(ul, ur, gconst, gconst, f, gate);
-        R F[NV];
-#pragma unroll
-        for (int c = 0; c < NV; ++c) F[c] = kind == 1 ? (c == 1 ? f[2] : (c == 2 ? f[1] : f[c])) : f[c];
-        if (kind == 0) {
-#pragma unroll
-          for (int c = 0; c < NV; ++c) fa[c * FA + slot_f] = F[c];
-          if (want_flux && fout[0]) {
-            const int64_t nf = (int64_t)g.na + 1;
-#pragma unroll
-            for (int c = 0; c < NV; ++c)
-              if (c < nvo) fout[0][((int64_t)(c * g.np + it) * g.nb + (y0 + j)) * nf + x0 + i] = F[c];
-          }
-        } else {
-#pragma unroll
-          for (int c = 0; c < NV; ++c) fb[c * FB + slot_f] = F[c];
-          if (want_flux && fout[1]) {
-#pragma unroll
-            for (int c = 0; c < NV; ++c)
-              if (c < nvo) fout[1][((int64_t)(c * g.np + it) * (g.nb + 1) + (y0 + j)) * g.na + x0 + i] = F[c];
-          }
-        }
-      }
-    }
-    if (stage_next) stage_end(it + 2);
-    if (__syncthreads_or(!waited_ok)) {  // in-plane fluxes complete; plane it+2 staged
-      if (tid == 0) st.status = kErrDeviceWait;
-      return false;
-    }
-    if (full && (at_x0 || at_x1 || at_y0 || at_y1)) {
-      // FP64 sums of the domain-boundary in-plane faces (edge tiles only)
-      for (int e = tid; e < 4 * 16 * NV; e += blockDim.x) {
-        const int q = e % (2 * 16 * NV);
-        const int side = q / (16 * NV), m = (q / NV) % 16, c = q % NV;
-        if (e < 2 * 16 * NV) {  // x faces of row m
-          if (m < by && (side ? at_x1 : at_x0))
-            bs_a[q] += (double)fa[c * FA + (side ? fa_edge16(m) : owner16_tid(0, m))];
-        } else {                // y faces of column m
-          if (m < ax && (side ? at_y1 : at_y0))
-            bs_b[q] += (double)fb[c * FB + (side ? 256 + m : owner16_tid(m, 0))];
-        }
-      }
-    }
-    R Fm[NV];
-#pragma unroll
-    for (int c = 0; c < NV; ++c) Fm[c] = R(0);
-    if (owner) {
-      const int li = (ob + 2) * S.pw + oa + S.xo;
-      if (it >= p0) {
-        hllc_cartesian_gated<NV>(Tprev, Bn, gconst, gconst, MD, Fm, gate);
-        if (want_flux && fout[MD]) {
-#pragma unroll
-          for (int c = 0; c < NV; ++c)
-            if (c < nvo) fout[MD][((int64_t)(c * (g.np + 1) + it) * g.nb + (y0 + ob)) * g.na + x0 + oa] = Fm[c];
-        }
-        if (it > p0) {
-          R un[NV];
-#pragma unroll
-          for (int c = 0; c < NV; ++c) un[c] = Pprev[c] - cu[MD] * (Fm[c] - Fprev[c]);
-          const int64_t off = (int64_t)(it - 1) * g.ps + (int64_t)(y0 + ob) * g.na + (x0 + oa);
-#pragma unroll
-          for (int c = 0; c < NV; ++c)
-            if (TFV_IN(25, off, g.cs) && TFV_OUTSIDE(60, Un + c * g.cs + off, A.ws_lo, A.ws_hi))
-              Un[c * g.cs + off] = un[c];
-          if (!physical_cell<R, NV>(un)) bad = true;
-          R w[DIM];
-          wave_speeds<R, DIM>(un, gconst, w);
-#pragma unroll
-          for (int k = 0; k < DIM; ++k) wmax[k] = fmax(wmax[k], w[k]);
-        }
-#pragma unroll
-        for (int c = 0; c < NV; ++c) Fprev[c] = Fm[c];
-      }
-      if (full) {
-        const int right = oa + 1 < ax ? tid + 1 : fa_edge16(ob);
-        const int top = ob + 1 < by ? owner16_tid(oa, ob + 1) : 256 + oa;
-#pragma unroll
-        for (int c = 0; c < NV; ++c)
-          Pprev[c] = rc[c * cplane + li] - cu[0] * (fa[c * FA + right] - fa[c * FA + tid]);
-#pragma unroll
-        for (int c = 0; c < NV; ++c)
-          Pprev[c] = Pprev[c] - cu[1] * (fb[c * FB + top] - fb[c * FB + tid]);
-      }
-#pragma unroll
-      for (int c = 0; c < NV; ++c) Tprev[c] = Tn[c];
-    }
-    if (it >= p0 && (it == 0 || it == g.np)) {  // march-axis boundary faces
-      FaceFlux<R, NV> ff;
-#pragma unroll
-      for (int c = 0; c < NV; ++c) ff.v[c] = owner ? Fm[c] : R(0);
-      march_boundary_sum<R, NV>(ff, red, bs_m + (it == 0 ? 0 : NV));
-    }
-  }
-
-  // tile epilogue: flags, wave maxima, boundary sums (the same fixed order as
-  // hydro_tile: rows / columns ascending)
-  int fl = (bad ? kFlagNonphysical : 0) | (gate ? kFlagGate : 0);
-  fl = block_or(fl, reinterpret_cast<int*>(red));
-  double wm[DIM];
-#pragma unroll
-  for (int k = 0; k < DIM; ++k) wm[k] = (double)block_max(owner ? wmax[k] : R(0), red);
-  __syncthreads();
-  if (tid == 0) {
-    double* out = A.t_bsum + (size_t)t * 15;
-    for (int c = 0; c < NV; ++c) {
-      double sa = 0.0, sb = 0.0;
-      for (int m = 0; m < 16; ++m) sa += bs_a[(1 * 16 + m) * NV + c] - bs_a[(0 * 16 + m) * NV + c];
-      for (int m = 0; m < 16; ++m) sb += bs_b[(1 * 16 + m) * NV + c] - bs_b[(0 * 16 + m) * NV + c];
-      out[0 * 5 + c] = sa;
-      out[1 * 5 + c] = sb;
-      out[MD * 5 + c] = bs_m[NV + c] - bs_m[c];
-    }
-    for (int k = 0; k < DIM; ++k) A.t_wmax[(size_t)t * 3 + k] = wm[k];
-    A.t_flags[t] = fl;
-    if (fl & (kFlagNonphysical | kFlagGate)) atomicOr(&st.fb_word, fl);
-  }
-  __syncthreads();
-  return true;
-}
-
 // TX, TY > 0: tile shape fixed at compile time (shared-memory offsets become
 // immediates); 0: taken from the launch arguments.
 template <typename R, int DIM, bool VARG, int LIM, int TX, int TY>
@@ -1383,9 +1017,8 @@ __global__ void __launch_bounds__(256, TFV_HYDRO_MIN_BLOCKS) hydro_kernel(StepAr
   // align by pointer arithmetic on the shared array (an integer round trip
   // would hide the address space and turn every shared access generic)
   unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
-  constexpr bool kOwnerFaces = OwnerFaces<R, DIM, VARG, TX, TY>::value;
   HydroSmem<R, DIM, VARG> S;
-  S.init(TX > 0 ? TX : A.tx, TY > 0 ? TY : A.ty, kOwnerFaces);
+  S.init(TX > 0 ? TX : A.tx, TY > 0 ? TY : A.ty);
   if (threadIdx.x == 0) {
     uint64_t* bars = smem_at<uint64_t>(smem, S.bar_off);
     for (int k = 0; k < 3; ++k) mbar_init(bars + k, 1);
@@ -1393,13 +1026,8 @@ __global__ void __launch_bounds__(256, TFV_HYDRO_MIN_BLOCKS) hydro_kernel(StepAr
   }
   __syncthreads();
   uint32_t bar_phase = 0;  // parity of the next completion of each slot's barrier
-  for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x) {
-    if constexpr (kOwnerFaces) {
-      if (!hydro_tile16<LIM>(A, t, smem, S, bar_phase)) break;
-    } else {
-      if (!hydro_tile<R, DIM, VARG, LIM>(A, t, smem, S, bar_phase)) break;
-    }
-  }
+  for (int t = A.t_begin + blockIdx.x; t < A.t_end; t += gridDim.x)
+    if (!hydro_tile<R, DIM, VARG, LIM>(A, t, smem, S, bar_phase)) break;
 }
 
 // --------------------------------------------------------------------------
