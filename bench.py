@@ -37,9 +37,9 @@ N = 256
 BYTES_PER_CELL = {"fp32": 40, "fp64": 80}  # read + write of 5 conserved values
 # DRAM bytes of one FP32 step-kernel launch per cell, from one ncu capture of
 # hydro_kernel<float,3,...,16,16> at 192^3 (dram__bytes_read.sum +
-# dram__bytes_write.sum = 154.01 + 107.46 MB for 7,077,888 cells); the traffic
+# dram__bytes_write.sum = 152.21 + 108.01 MB for 7,077,888 cells); the traffic
 # grows in proportion to the cells a launch processes.
-TRAFFIC_PER_CELL = (154.01e6 + 107.46e6) / 192 ** 3
+TRAFFIC_PER_CELL = (152.21e6 + 108.01e6) / 192 ** 3
 
 
 def explosion_3d(n, nz=None):
