@@ -325,15 +325,14 @@ __global__ void __launch_bounds__(kMThreads) metric_prim_kernel(MArgs<R> A) {
 // Rusanov flux of face f (padded cells f and f + 1 with their slopes),
 // weighted by the face area, and the upwind fraction transport
 // (torchFiniteVolume.py:160-226).
-// The area-weighted flux (W[NV]) and fraction transport (T[2]) of face f.
 template <typename R, int DIM, int D>
-__device__ __forceinline__ void face_flux(const MArgs<R>& A, int f, const MIdx& c,
+__device__ __forceinline__ void emit_face(const MArgs<R>& A, int f, const MIdx& c, int64_t idx,
                                           const MCell<R, DIM + 2>& cl,
-                                          const MCell<R, DIM + 2>& cr, const R* sl, const R* sr,
-                                          R* W, R* T) {
+                                          const MCell<R, DIM + 2>& cr, const R* sl, const R* sr) {
   constexpr int NV = DIM + 2;
   constexpr int d = D;
   const int n = A.n[d];
+  const int64_t nf = A.nf[d];
   R left[NV], right[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
@@ -371,32 +370,19 @@ __device__ __forceinline__ void face_flux(const MArgs<R>& A, int f, const MIdx& 
   const R speed = np_max(fabs(vl) + sqrt((gl * left[NV - 1]) / left[0]),
                          fabs(vr) + sqrt((gr * right[NV - 1]) / right[0]));
   const R ar = area<R, DIM>(A, d, f, c);
+  R* W = A.W[d];
   R flux0 = R(0);
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
     const R flux = ((fl[v] + fr[v]) - (ur[v] - ul[v]) * speed) * R(0.5);
     if (v == 0) flux0 = flux;
-    W[v] = flux * ar;
+    W[v * nf + idx] = flux * ar;
   }
   // first-order upwind transport of the fractions (torchFiniteVolume.py:223-226)
-#pragma unroll
-  for (int q = 0; q < 2; ++q) {
+  for (int q = 0; q < A.nfrac; ++q) {
     const R up = flux0 >= R(0) ? cl.q[q] : cr.q[q];
-    T[q] = q < A.nfrac ? (flux0 * up) * ar : R(0);
+    A.T[d][q * nf + idx] = (flux0 * up) * ar;
   }
-}
-
-template <typename R, int DIM, int D>
-__device__ __forceinline__ void emit_face(const MArgs<R>& A, int f, const MIdx& c, int64_t idx,
-                                          const MCell<R, DIM + 2>& cl,
-                                          const MCell<R, DIM + 2>& cr, const R* sl, const R* sr) {
-  constexpr int NV = DIM + 2;
-  const int64_t nf = A.nf[D];
-  R W[NV], T[2];
-  face_flux<R, DIM, D>(A, f, c, cl, cr, sl, sr, W, T);
-#pragma unroll
-  for (int v = 0; v < NV; ++v) A.W[D][v * nf + idx] = W[v];
-  for (int q = 0; q < A.nfrac; ++q) A.T[D][q * nf + idx] = T[q];
 }
 
 template <typename R, int DIM, int D>
@@ -604,275 +590,6 @@ __global__ void __launch_bounds__(kMThreads) metric_update_kernel(MArgs<R> A, in
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) A.Uout[v * A.nc + off] = out[v];
-  }
-  if (err) atomicOr(A.err, err);
-}
-
-// -- 3b. one fused SSPRK2 stage: faces, divergence, stage combination --------
-// The work of metric_face_kernel / metric_face_march_kernel,
-// metric_update_kernel and metric_outward_kernel in one pass, for 2D and 3D
-// grids (1D sessions keep the separate kernels).  A CTA of 256 threads owns
-// a tile of columns (3D: 32 along x by 8 along y; 2D: 256 along x) and
-// marches along the last axis through a chunk of cells.  Each thread owns
-// one column: it forms its cell's slope along every direction once, the flux
-// of its low x face (the high one is the next lane's low face, passed by a
-// warp shuffle) and of its low y face (the high one is the next row's, passed
-// through shared memory), and the march-axis faces from a sliding window of
-// padded cells in registers.  Faces, slopes and the divergence use the
-// functions and the operation order of the separate kernels (x, y, z faces of
-// a cell in that order), so the states are the same bit for bit.  Outward
-// (boundary-face) sums go to per-CTA partials in a fixed order.
-// Reference: python/cfdSolver/torchFiniteVolume.py:160-276.
-constexpr int kMStageThreads = 256;
-constexpr int kMStageBlocks = 4096;  // partial-sum records of the fused stage
-
-template <int DIM>
-struct MStageShape {
-  static constexpr int TX = DIM == 3 ? 32 : 256;  // columns along x
-  static constexpr int TY = DIM == 3 ? 8 : 1;     // rows along y (3D)
-};
-
-// slope of padded cell j along D at column c (torchFiniteVolume.py:146-153):
-// interior padded cells from their neighbours; the low / high ghost of a
-// periodic direction takes the last / first cell's slope; other ghosts none
-template <typename R, int NV, int D>
-__device__ __forceinline__ int padded_slope(const MArgs<R>& A, int j, const MIdx& c, R* s) {
-  const int n = A.n[D];
-  int j0;
-  if (j >= 1 && j <= n) {
-    j0 = j - 1;
-  } else if (A.periodic[D]) {
-    j0 = j == 0 ? n - 1 : 0;
-  } else {
-#pragma unroll
-    for (int v = 0; v < NV; ++v) s[v] = R(0);
-    return 0;
-  }
-  int err = 0;
-  MCell<R, NV> a, b, e;
-  err |= padded_cell<R, NV, D>(A, j0, c, a);
-  err |= padded_cell<R, NV, D>(A, j0 + 1, c, b);
-  err |= padded_cell<R, NV, D>(A, j0 + 2, c, e);
-  cell_slope<R, NV>(a, b, e, A.limiter, s);
-  return err;
-}
-
-template <typename R, int NV>
-__device__ __forceinline__ void zero_slope(R* s) {
-#pragma unroll
-  for (int v = 0; v < NV; ++v) s[v] = R(0);
-}
-
-template <typename R, int DIM>
-__global__ void __launch_bounds__(kMStageThreads) metric_stage_kernel(MArgs<R> A, int stage) {
-  constexpr int NV = DIM + 2;
-  constexpr int M = DIM - 1;  // marching direction
-  constexpr int TX = MStageShape<DIM>::TX, TY = MStageShape<DIM>::TY;
-  constexpr int NW = NV + 2;  // a face: NV fluxes + 2 fraction transports
-  __shared__ R s_sy[DIM == 3 ? TY * TX * NV : 1];
-  __shared__ R s_wy[DIM == 3 ? TY * TX * NW : 1];
-  __shared__ double red[32];
-  const int tid = threadIdx.x;
-  const int col = DIM == 3 ? (tid & 31) : tid;
-  const int row = DIM == 3 ? (tid >> 5) : 0;
-  const int lane = tid & 31;
-  const int nx = A.n[0], ny = DIM == 3 ? A.n[1] : 1, nm = A.n[M];
-  const int tiles_x = (nx + TX - 1) / TX, tiles_y = (ny + TY - 1) / TY;
-  const int CH = A.chunk;
-  const int nchunks = (nm + CH - 1) / CH;
-  const int64_t ntiles = (int64_t)tiles_x * tiles_y;
-  const int64_t items = ntiles * nchunks;
-  const bool fo = A.first_order != 0;
-  const R dt = R(A.dt);
-  double acc[NV];
-#pragma unroll
-  for (int v = 0; v < NV; ++v) acc[v] = 0.0;
-  int err = 0;
-  for (int64_t item = blockIdx.x; item < items; item += gridDim.x) {
-    const int tile = (int)(item % ntiles);
-    const int ch = (int)(item / ntiles);
-    const int i = (tile % tiles_x) * TX + col;
-    const int j = (tile / tiles_x) * TY + row;
-    const bool active = i < nx && j < ny;
-    // inactive threads work on a clamped column so that every load stays in
-    // range; they take part in the shuffles and barriers and store nothing
-    MIdx c;
-    c.i = min(i, nx - 1);
-    c.j = DIM == 3 ? min(j, ny - 1) : 0;
-    c.k = 0;
-    const int k0 = ch * CH, k1 = min(k0 + CH, nm);
-    // march window: own = padded cell m + 1 (cell m) with slope s_own
-    MCell<R, NV> own, up;
-    R s_own[NV], wz_lo[NW], wz_hi[NW];
-    {
-      R s_lo[NV];
-      MCell<R, NV> lo;
-      err |= padded_cell<R, NV, M>(A, k0, c, lo);      // below the first cell
-      err |= padded_cell<R, NV, M>(A, k0 + 1, c, own);  // the first cell
-      if (fo) {
-        zero_slope<R, NV>(s_lo);
-        zero_slope<R, NV>(s_own);
-      } else {
-        err |= padded_slope<R, NV, M>(A, k0, c, s_lo);
-        err |= padded_slope<R, NV, M>(A, k0 + 1, c, s_own);
-      }
-      face_flux<R, DIM, M>(A, k0, c, lo, own, s_lo, s_own, wz_lo, wz_lo + NV);
-    }
-    for (int m = k0; m < k1; ++m) {
-      MIdx co = c;
-      if (M == 1) co.j = m; else co.k = m;
-      const int64_t off = off_of(co.i, co.j, co.k, A.n);
-      R kk[NV], kq[2];
-#pragma unroll
-      for (int v = 0; v < NV; ++v) kk[v] = A.K[v * A.nc + off];
-      kq[0] = kq[1] = R(0);
-      const R vol = volume<R, DIM>(A, co);
-      // ---- x faces (direction 0)
-      {
-        MCell<R, NV> xm, xp;
-        err |= padded_cell<R, NV, 0>(A, co.i, co, xm);      // cell i - 1 (or ghost)
-        err |= padded_cell<R, NV, 0>(A, co.i + 2, co, xp);  // cell i + 1 (or ghost)
-        R sx[NV], sxm[NV];
-        if (fo) zero_slope<R, NV>(sx);
-        else cell_slope<R, NV>(xm, own, xp, A.limiter, sx);
-#pragma unroll
-        for (int v = 0; v < NV; ++v) sxm[v] = __shfl_up_sync(0xffffffffu, sx[v], 1);
-        if (lane == 0) {
-          if (fo) zero_slope<R, NV>(sxm);
-          else err |= padded_slope<R, NV, 0>(A, co.i, co, sxm);
-        }
-        R wlo[NW], whi[NW];
-        face_flux<R, DIM, 0>(A, co.i, co, xm, own, sxm, sx, wlo, wlo + NV);
-#pragma unroll
-        for (int v = 0; v < NW; ++v) whi[v] = __shfl_down_sync(0xffffffffu, wlo[v], 1);
-        if (lane == 31 || co.i + 1 >= nx) {
-          R sxp[NV];
-          if (fo) zero_slope<R, NV>(sxp);
-          else err |= padded_slope<R, NV, 0>(A, co.i + 2, co, sxp);
-          face_flux<R, DIM, 0>(A, co.i + 1, co, own, xp, sx, sxp, whi, whi + NV);
-        }
-#pragma unroll
-        for (int v = 0; v < NV; ++v) kk[v] = kk[v] - (whi[v] - wlo[v]) / vol;
-        for (int q = 0; q < A.nfrac; ++q) kq[q] = kq[q] - (whi[NV + q] - wlo[NV + q]) / vol;
-        if (active && co.i == 0) {
-#pragma unroll
-          for (int v = 0; v < NV; ++v) acc[v] -= (double)wlo[v];
-        }
-        if (active && co.i == nx - 1) {
-#pragma unroll
-          for (int v = 0; v < NV; ++v) acc[v] += (double)whi[v];
-        }
-      }
-      // ---- y faces (direction 1; in 2D y is the marching axis)
-      if constexpr (DIM == 3) {
-        MCell<R, NV> ym, yp;
-        err |= padded_cell<R, NV, 1>(A, co.j, co, ym);
-        err |= padded_cell<R, NV, 1>(A, co.j + 2, co, yp);
-        R sy[NV], sym[NV];
-        if (fo) zero_slope<R, NV>(sy);
-        else cell_slope<R, NV>(ym, own, yp, A.limiter, sy);
-#pragma unroll
-        for (int v = 0; v < NV; ++v) s_sy[(row * TX + col) * NV + v] = sy[v];
-        __syncthreads();
-        if (row > 0) {
-#pragma unroll
-          for (int v = 0; v < NV; ++v) sym[v] = s_sy[((row - 1) * TX + col) * NV + v];
-        } else if (fo) {
-          zero_slope<R, NV>(sym);
-        } else {
-          err |= padded_slope<R, NV, 1>(A, co.j, co, sym);
-        }
-        R wlo[NW], whi[NW];
-        face_flux<R, DIM, 1>(A, co.j, co, ym, own, sym, sy, wlo, wlo + NV);
-#pragma unroll
-        for (int v = 0; v < NW; ++v) s_wy[(row * TX + col) * NW + v] = wlo[v];
-        __syncthreads();
-        if (row < TY - 1 && co.j + 1 < ny) {
-#pragma unroll
-          for (int v = 0; v < NW; ++v) whi[v] = s_wy[((row + 1) * TX + col) * NW + v];
-        } else {
-          R syp[NV];
-          if (fo) zero_slope<R, NV>(syp);
-          else err |= padded_slope<R, NV, 1>(A, co.j + 2, co, syp);
-          face_flux<R, DIM, 1>(A, co.j + 1, co, own, yp, sy, syp, whi, whi + NV);
-        }
-#pragma unroll
-        for (int v = 0; v < NV; ++v) kk[v] = kk[v] - (whi[v] - wlo[v]) / vol;
-        for (int q = 0; q < A.nfrac; ++q) kq[q] = kq[q] - (whi[NV + q] - wlo[NV + q]) / vol;
-        if (active && co.j == 0) {
-#pragma unroll
-          for (int v = 0; v < NV; ++v) acc[v] -= (double)wlo[v];
-        }
-        if (active && co.j == ny - 1) {
-#pragma unroll
-          for (int v = 0; v < NV; ++v) acc[v] += (double)whi[v];
-        }
-      }
-      // ---- march-axis faces: the high face of the own cell from the window
-      {
-        err |= padded_cell<R, NV, M>(A, m + 2, c, up);  // cell m + 1 (or ghost)
-        R s_up[NV];
-        if (fo) {
-          zero_slope<R, NV>(s_up);
-        } else if (m + 2 <= nm) {
-          MCell<R, NV> nxt;
-          err |= padded_cell<R, NV, M>(A, m + 3, c, nxt);
-          cell_slope<R, NV>(own, up, nxt, A.limiter, s_up);
-        } else {
-          err |= padded_slope<R, NV, M>(A, m + 2, c, s_up);
-        }
-        face_flux<R, DIM, M>(A, m + 1, c, own, up, s_own, s_up, wz_hi, wz_hi + NV);
-#pragma unroll
-        for (int v = 0; v < NV; ++v) kk[v] = kk[v] - (wz_hi[v] - wz_lo[v]) / vol;
-        for (int q = 0; q < A.nfrac; ++q) kq[q] = kq[q] - (wz_hi[NV + q] - wz_lo[NV + q]) / vol;
-        if (active && m == 0) {
-#pragma unroll
-          for (int v = 0; v < NV; ++v) acc[v] -= (double)wz_lo[v];
-        }
-        if (active && m == nm - 1) {
-#pragma unroll
-          for (int v = 0; v < NV; ++v) acc[v] += (double)wz_hi[v];
-        }
-#pragma unroll
-        for (int v = 0; v < NV; ++v) s_own[v] = s_up[v];
-#pragma unroll
-        for (int v = 0; v < NW; ++v) wz_lo[v] = wz_hi[v];
-      }
-      // ---- the SSPRK2 stage combination (as metric_update_kernel)
-      if (active) {
-        R out[NV], oq[2];
-        if (stage == 1) {
-#pragma unroll
-          for (int v = 0; v < NV; ++v) out[v] = A.U[v * A.nc + off] + dt * kk[v];
-          const R rho0 = A.U[off];
-          for (int q = 0; q < A.nfrac; ++q)
-            oq[q] = (rho0 * A.Q[q][off] + dt * kq[q]) / out[0];
-        } else {
-#pragma unroll
-          for (int v = 0; v < NV; ++v)
-            out[v] = R(0.5) * ((A.U0[v * A.nc + off] + A.Us[v * A.nc + off]) + dt * kk[v]);
-          const R rho0 = A.U0[off], rhos = A.Us[off];
-          for (int q = 0; q < A.nfrac; ++q)
-            oq[q] = (R(0.5) * ((rho0 * A.Q0[q][off] + rhos * A.Qs[q][off]) + dt * kq[q])) / out[0];
-        }
-        if (!physical_cell<R, NV>(out)) err |= kMErrNonphysical;
-        const R tol = Exact<R>::value ? R(1e-12) : R(1e-5);
-        for (int q = 0; q < A.nfrac; ++q) {
-          if (oq[q] < -tol || oq[q] > R(1) + tol) err |= kMErrFraction;
-          oq[q] = np_min(np_max(oq[q], R(0)), R(1));  // np.clip
-          A.Qout[q][off] = oq[q];
-        }
-#pragma unroll
-        for (int v = 0; v < NV; ++v) A.Uout[v * A.nc + off] = out[v];
-      }
-      own = up;
-    }
-    if (DIM == 3) __syncthreads();  // shared rows free before the next item
-  }
-#pragma unroll
-  for (int v = 0; v < NV; ++v) {
-    const double t = block_sum(acc[v], red);
-    if (threadIdx.x == 0) A.part[blockIdx.x * 8 + v] = t;
   }
   if (err) atomicOr(A.err, err);
 }

@@ -220,36 +220,6 @@ struct Driver {
     TFV_MCUDA(launch(kMOpOutward, 0, g));
     return reduce(slot_outward, g);
   }
-  // one fused SSPRK2 stage of a 2D / 3D grid: K of v (primitives reused from
-  // the dt pass when they are v's), then faces, divergence and the stage
-  // combination into A.Uout in one kernel, with its outward partial sums
-  int fused_stage(const View& v, int stage, bool first_order, int slot_source,
-                  int slot_outward) {
-    A.first_order = first_order ? 1 : 0;
-    if (prim_state == v.u && prim_slot >= 0) {
-      set_input(v);
-      if (prim_slot != slot_source)
-        TFV_MCUDA(cudaMemcpyAsync(res + slot_source * 8, res + prim_slot * 8, 8 * sizeof(double),
-                                  cudaMemcpyDeviceToDevice, s));
-    } else {
-      int r = prim(v, slot_source);
-      if (r) return r;
-    }
-    // columns of 32 x 8 (3D) or 256 (2D) cells, marched along the last axis
-    // in chunks sized for about four CTAs per SM (at least 16 cells each)
-    const int tx = m->dim == 3 ? 32 : 256, ty = m->dim == 3 ? 8 : 1;
-    const int nm = m->cfg.n[m->dim - 1];
-    const int64_t tiles = (int64_t)((m->cfg.n[0] + tx - 1) / tx) *
-                          (m->dim == 3 ? (m->cfg.n[1] + ty - 1) / ty : 1);
-    const int64_t want = (int64_t)m->sms * 4;
-    const int chunk =
-        (int)std::min<int64_t>(nm, std::max<int64_t>(16, (nm * tiles + want - 1) / want));
-    A.chunk = chunk;
-    const int64_t items = tiles * ((nm + chunk - 1) / chunk);
-    const int grid = (int)std::min<int64_t>(items, kMStagePartBlocks);
-    TFV_MCUDA(launch(kMOpStage, stage, grid));
-    return reduce(slot_outward, grid);
-  }
   // largest CFL rate of the state v; sets *rate (NaN when not finite) and err bits
   int rate(const View& v, double* out, int32_t* err) {
     TFV_MCUDA(cudaMemsetAsync(A.rate_max, 0, sizeof(unsigned long long), s));
@@ -338,24 +308,20 @@ int metric_step(tfv_metric* m) {
     }
     // SSPRK2, then the same at first order (torchFiniteVolume.py:234-276)
     int used = -1;
-    const bool fused = m->dim >= 2;  // one kernel per stage; 1D keeps the separate kernels
     for (int fo = 0; fo < 2 && used < 0; ++fo) {
       TFV_MCUDA(cudaMemsetAsync(D.A.err, 0, sizeof(int32_t), D.s));
+      if ((r = D.rhs(old, fo == 1, kSlotSource1, kSlotOutward1))) return r;
+      D.set_input(old);
       D.A.Uout = (R*)stage.u;
       D.A.Qout[0] = (R*)stage.q[0];
       D.A.Qout[1] = (R*)stage.q[1];
-      if (fused) {
-        if ((r = D.fused_stage(old, 1, fo == 1, kSlotSource1, kSlotOutward1))) return r;
-      } else {
-        if ((r = D.rhs(old, fo == 1, kSlotSource1, kSlotOutward1))) return r;
-        D.set_input(old);
-        TFV_MCUDA(D.launch(kMOpUpdate, 1, grid_for(m, m->nc)));
-      }
+      TFV_MCUDA(D.launch(kMOpUpdate, 1, grid_for(m, m->nc)));
       int32_t e1 = 0;
       TFV_MCUDA(cudaMemcpyAsync(&e1, D.A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, D.s));
       TFV_MCUDA(cudaStreamSynchronize(D.s));
       if ((r = D.boundary_error(e1))) return r;
       if (e1 & (kMErrNonphysical | kMErrFraction)) continue;
+      if ((r = D.rhs(stage, fo == 1, kSlotSource2, kSlotOutward2))) return r;
       D.A.U0 = (const R*)old.u;
       D.A.Q0[0] = (const R*)old.q[0];
       D.A.Q0[1] = (const R*)old.q[1];
@@ -365,12 +331,7 @@ int metric_step(tfv_metric* m) {
       D.A.Uout = (R*)next.u;
       D.A.Qout[0] = (R*)next.q[0];
       D.A.Qout[1] = (R*)next.q[1];
-      if (fused) {
-        if ((r = D.fused_stage(stage, 2, fo == 1, kSlotSource2, kSlotOutward2))) return r;
-      } else {
-        if ((r = D.rhs(stage, fo == 1, kSlotSource2, kSlotOutward2))) return r;
-        TFV_MCUDA(D.launch(kMOpUpdate, 2, grid_for(m, m->nc)));
-      }
+      TFV_MCUDA(D.launch(kMOpUpdate, 2, grid_for(m, m->nc)));
       int32_t e2 = 0;
       TFV_MCUDA(cudaMemcpyAsync(&e2, D.A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, D.s));
       TFV_MCUDA(cudaStreamSynchronize(D.s));
@@ -518,13 +479,13 @@ int tfv_metric_create(int32_t precision, const tfv_metric_config* cfg, const dou
   m->off_p = take(st);
   m->off_g = take(sc);
   m->off_k = take(st);
-  if (m->dim == 1) {  // face arrays: only the separate face / update kernels of 1D
-    m->off_w[0] = take(m->esz * m->nv * m->nf[0]);
-    m->off_t[0] = take(m->esz * 2 * m->nf[0]);
+  for (int d = 0; d < m->dim; ++d) {
+    m->off_w[d] = take(m->esz * m->nv * m->nf[d]);
+    m->off_t[d] = take(m->esz * 2 * m->nf[d]);
   }
   m->off_faces = take(sizeof(MFace<double>) * 6);
   m->off_fac = take(m->esz * m->factors.size());
-  m->off_part = take(sizeof(double) * std::max(kMReduceBlocks, kMStagePartBlocks) * 8);
+  m->off_part = take(sizeof(double) * kMReduceBlocks * 8);
   m->off_res = take(sizeof(double) * kSlots * 8);
   m->off_rate = take(sizeof(unsigned long long));
   m->off_err = take(sizeof(int32_t));

@@ -16,12 +16,7 @@ enum : int {
   kMOpRate = 4,      // CFL rate maximum
   kMOpReact = 5,     // arg = 0: reaction half into Uout; 1: closing half in place + source partials
   kMOpIntegral = 6,  // partials of the state integral
-  kMOpStage = 7,     // arg = SSPRK2 stage (1 or 2): fused faces + update + outward partials (2D/3D)
 };
-
-// CTA size and the largest grid (partial-sum records) of the fused stage
-constexpr int kMStageThreadsHost = 256;
-constexpr int kMStagePartBlocks = 4096;
 
 cudaError_t metric_launch_f64(int op, int dim, const MArgs<double>& A, int arg, int grid,
                               cudaStream_t s);
