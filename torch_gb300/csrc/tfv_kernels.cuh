@@ -1246,22 +1246,34 @@ __global__ void __launch_bounds__(256) waves_kernel(StepArgs A, int sums) {
 #pragma unroll
     for (int c = 0; c < NV; ++c) sum[c] = 0.0;
     if (owner) {
-      for (int p = T.p0; p < T.p1; ++p) {
-        const int64_t off = (int64_t)p * g.ps + (int64_t)b * g.na + a;
-        if (!TFV_IN(27, off, g.cs)) continue;
-        R u[NV];
+      // planes in groups of four: every load of a group is issued before the
+      // first is used (one column per thread leaves little other parallelism);
+      // the sums still run plane by plane in order
+      constexpr int G4 = 4;
+      for (int p = T.p0; p < T.p1; p += G4) {
+        R u[G4][NV];
+        R gc[G4];
 #pragma unroll
-        for (int c = 0; c < NV; ++c) u[c] = U[c * g.cs + off];
-        if (sums) {
+        for (int q = 0; q < G4; ++q) {
+          const int64_t off = (int64_t)(p + q) * g.ps + (int64_t)b * g.na + a;
+          const bool in = p + q < T.p1 && TFV_IN(27, off, g.cs);
 #pragma unroll
-          for (int c = 0; c < NV; ++c) sum[c] += (double)u[c];
+          for (int c = 0; c < NV; ++c) u[q][c] = in ? U[c * g.cs + off] : R(1);
+          gc[q] = VARG ? (in ? gam[off] : R(1.4)) : desc_gamma(d, R(0));
         }
-        const R gc = VARG ? gam[off] : desc_gamma(d, R(0));
-        if (!physical_cell<R, NV>(u)) bad = true;
-        R w[DIM];
-        wave_speeds<R, DIM>(u, gc, w);
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) wmax[k] = fmax(wmax[k], w[k]);
+        for (int q = 0; q < G4; ++q) {
+          if (p + q >= T.p1) break;
+          if (sums) {
+#pragma unroll
+            for (int c = 0; c < NV; ++c) sum[c] += (double)u[q][c];
+          }
+          if (!physical_cell<R, NV>(u[q])) bad = true;
+          R w[DIM];
+          wave_speeds<R, DIM>(u[q], gc[q], w);
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) wmax[k] = fmax(wmax[k], w[k]);
+        }
       }
     }
     int fl = block_or(bad ? kFlagNonphysical : 0, reinterpret_cast<int*>(red));
