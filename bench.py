@@ -988,10 +988,10 @@ def main():
         barrier()
         return s2.elapsed_time(e2) / (e2e_steps * len(lanes))
 
-    # five timed trials of e2e_steps steps of every session; the median is
+    # seven timed trials of e2e_steps steps of every session; the median is
     # reported (the host link is shared with the other GPU on the same CPU,
-    # so single trials vary) with all five and the link rates after them
-    e2e_samples = [e2e_trial() for _ in range(5)]
+    # so single trials vary) with all seven and the link rates after them
+    e2e_samples = [e2e_trial() for _ in range(7)]
     e2e_ms = statistics.median(e2e_samples)
     e2e_ms = max_over_ranks(e2e_ms, dist, "cuda")
     link_after = link_rates(lanes[0]["host_in"], lanes[0]["eng"].current(), lanes[0]["host_out"])
