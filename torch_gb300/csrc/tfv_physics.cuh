@@ -74,6 +74,24 @@ template <typename R, int DIM, int LIM>
 __device__ __forceinline__ R limited_slope(R um, R uc, R up) {
   const R minus = uc - um;
   const R plus = up - uc;
+  if constexpr (!Exact<R>::value && (LIM == 2 || LIM == 3)) {
+    // single precision, MINBEE and Superbee: phi(r) * plus with r = minus /
+    // plus, multiplied through by |plus| (no division): with s = sign(plus),
+    // a = s * minus and b = |plus|, MINBEE is s * max(0, min(a, b)) and
+    // Superbee s * max(0, max(min(2a, b), min(a, 2b))).  Equal to the
+    // reference's form except where |plus| < 1e-14, whose guard changes the
+    // result by less than 2e-14 (below single-precision resolution);
+    // NaN still propagates through the NaN-propagating min / max.
+    const R s = copysignf(1.0f, plus);
+    const R a = minus * s;
+    const R b = fabsf(plus);
+    R t;
+    if (LIM == 2)
+      t = np_max(R(0), np_min(a, b));
+    else
+      t = np_max(R(0), np_max(np_min(a + a, b), np_min(a, b + b)));
+    return t * s;
+  }
   const R r = dv(minus, guarded(plus, R(kGuard)));
   R phi;
   if (LIM == 1) {  // Albada
