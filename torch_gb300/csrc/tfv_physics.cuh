@@ -92,6 +92,15 @@ __device__ __forceinline__ R limited_slope(R um, R uc, R up) {
       t = np_max(R(0), np_max(np_min(a + a, b), np_min(a, b + b)));
     return t * s;
   }
+  if constexpr (!Exact<R>::value && LIM == 0) {
+    // single precision, VanLeer: with r = minus / plus > 0,
+    // phi(r) * plus = 2 minus plus / (minus + plus); zero for r <= 0.  One
+    // reciprocal instead of two; the guard of tiny |plus| makes a difference
+    // below single-precision resolution; NaN inputs give NaN.
+    const R mp = minus * plus;
+    const R v = (mp + mp) * rcp(minus + plus);
+    return mp > R(0) ? v : (mp == mp ? R(0) : mp);
+  }
   const R r = dv(minus, guarded(plus, R(kGuard)));
   R phi;
   if (LIM == 1) {  // Albada
