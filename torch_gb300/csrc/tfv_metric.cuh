@@ -325,14 +325,15 @@ __global__ void __launch_bounds__(kMThreads) metric_prim_kernel(MArgs<R> A) {
 // Rusanov flux of face f (padded cells f and f + 1 with their slopes),
 // weighted by the face area, and the upwind fraction transport
 // (torchFiniteVolume.py:160-226).
+// The area-weighted flux (W[NV]) and fraction transport (T[2]) of face f.
 template <typename R, int DIM, int D>
-__device__ __forceinline__ void emit_face(const MArgs<R>& A, int f, const MIdx& c, int64_t idx,
+__device__ __forceinline__ void face_flux(const MArgs<R>& A, int f, const MIdx& c,
                                           const MCell<R, DIM + 2>& cl,
-                                          const MCell<R, DIM + 2>& cr, const R* sl, const R* sr) {
+                                          const MCell<R, DIM + 2>& cr, const R* sl, const R* sr,
+                                          R* W, R* T) {
   constexpr int NV = DIM + 2;
   constexpr int d = D;
   const int n = A.n[d];
-  const int64_t nf = A.nf[d];
   R left[NV], right[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
@@ -370,19 +371,32 @@ __device__ __forceinline__ void emit_face(const MArgs<R>& A, int f, const MIdx& 
   const R speed = np_max(fabs(vl) + sqrt((gl * left[NV - 1]) / left[0]),
                          fabs(vr) + sqrt((gr * right[NV - 1]) / right[0]));
   const R ar = area<R, DIM>(A, d, f, c);
-  R* W = A.W[d];
   R flux0 = R(0);
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
     const R flux = ((fl[v] + fr[v]) - (ur[v] - ul[v]) * speed) * R(0.5);
     if (v == 0) flux0 = flux;
-    W[v * nf + idx] = flux * ar;
+    W[v] = flux * ar;
   }
   // first-order upwind transport of the fractions (torchFiniteVolume.py:223-226)
-  for (int q = 0; q < A.nfrac; ++q) {
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
     const R up = flux0 >= R(0) ? cl.q[q] : cr.q[q];
-    A.T[d][q * nf + idx] = (flux0 * up) * ar;
+    T[q] = q < A.nfrac ? (flux0 * up) * ar : R(0);
   }
+}
+
+template <typename R, int DIM, int D>
+__device__ __forceinline__ void emit_face(const MArgs<R>& A, int f, const MIdx& c, int64_t idx,
+                                          const MCell<R, DIM + 2>& cl,
+                                          const MCell<R, DIM + 2>& cr, const R* sl, const R* sr) {
+  constexpr int NV = DIM + 2;
+  const int64_t nf = A.nf[D];
+  R W[NV], T[2];
+  face_flux<R, DIM, D>(A, f, c, cl, cr, sl, sr, W, T);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) A.W[D][v * nf + idx] = W[v];
+  for (int q = 0; q < A.nfrac; ++q) A.T[D][q * nf + idx] = T[q];
 }
 
 template <typename R, int DIM, int D>
@@ -461,8 +475,9 @@ __device__ __forceinline__ int64_t face_off(int d, int f, const MIdx& c, const i
   return ((int64_t)f * n[1] + c.j) * n[0] + c.i;
 }
 
-// Faces of direction D (y or z) marched in chunks of `chunk` along D by one
-// thread each, threads adjacent along x: a sliding window of padded cells
+// Faces of direction D marched in chunks of `chunk` along D by one thread
+// each (threads adjacent along x, or along y for the x faces of 2D / 3D
+// grids): a sliding window of padded cells
 // f, f + 1, f + 2 and the slope of each padded cell formed once, so a face
 // costs one new cell load, one slope and one flux.  The values are those of
 // metric_face_kernel.
@@ -470,7 +485,6 @@ template <typename R, int DIM, int D>
 __global__ void __launch_bounds__(kMThreads) metric_face_march_kernel(MArgs<R> A) {
   const int chunk = A.chunk;
   constexpr int NV = DIM + 2;
-  static_assert(D >= 1, "x faces use metric_face_kernel");
   const int n = A.n[D];
   const int nchunks = (n + chunk) / chunk;  // faces 0..n
   const int64_t ntr = A.nc / n;             // cells of a plane normal to D
@@ -483,7 +497,11 @@ __global__ void __launch_bounds__(kMThreads) metric_face_march_kernel(MArgs<R> A
     const int ch = (int)(t / ntr);
     MIdx c;
     c.i = (int)(tr % A.n[0]);
-    if (D == 1) {
+    if (D == 0) {  // threads adjacent along y; each marches its own row
+      c.i = 0;
+      c.j = (int)(tr % A.n[1]);
+      c.k = (int)(tr / A.n[1]);
+    } else if (D == 1) {
       c.j = 0;
       c.k = (int)(tr / A.n[0]);
     } else {
@@ -590,6 +608,155 @@ __global__ void __launch_bounds__(kMThreads) metric_update_kernel(MArgs<R> A, in
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) A.Uout[v * A.nc + off] = out[v];
+  }
+  if (err) atomicOr(A.err, err);
+}
+
+// -- 3b. last-direction faces fused with the stage update ---------------------
+// The faces of the marching direction D = DIM - 1 (z in 3D, y in 2D) formed
+// as metric_face_march_kernel forms them, each thread marching one column
+// through a chunk of cells; with the low and high face of a cell in
+// registers, the thread finishes that cell's divergence (x and y faces read
+// from their arrays, then the D faces: the order of metric_update_kernel)
+// and its SSPRK2 stage combination at once, so the D-face arrays are never
+// written except on the two boundary planes (read by the outward sums) and
+// the separate update pass is gone.  Values equal those of the separate
+// kernels bit for bit (python/cfdSolver/torchFiniteVolume.py:160-276).
+template <typename R, int DIM>
+__device__ __forceinline__ int update_cell(const MArgs<R>& A, const MIdx& co, const R* wlo,
+                                           const R* whi, int stage, R dt) {
+  constexpr int NV = DIM + 2;
+  constexpr int D = DIM - 1;
+  int err = 0;
+  const int64_t off = off_of(co.i, co.j, co.k, A.n);
+  const R vol = volume<R, DIM>(A, co);
+  R k[NV], kq[2] = {R(0), R(0)};
+#pragma unroll
+  for (int v = 0; v < NV; ++v) k[v] = A.K[v * A.nc + off];
+  const int cc[3] = {co.i, co.j, co.k};
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    if (d == D) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) k[v] = k[v] - (whi[v] - wlo[v]) / vol;
+      for (int q = 0; q < A.nfrac; ++q) kq[q] = kq[q] - (whi[NV + q] - wlo[NV + q]) / vol;
+    } else {
+      const int64_t lo = face_off(d, cc[d], co, A.n), hi = face_off(d, cc[d] + 1, co, A.n);
+      const int64_t nf = A.nf[d];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) k[v] = k[v] - (A.W[d][v * nf + hi] - A.W[d][v * nf + lo]) / vol;
+      for (int q = 0; q < A.nfrac; ++q)
+        kq[q] = kq[q] - (A.T[d][q * nf + hi] - A.T[d][q * nf + lo]) / vol;
+    }
+  }
+  R out[NV], oq[2];
+  if (stage == 1) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) out[v] = A.U[v * A.nc + off] + dt * k[v];
+    const R rho0 = A.U[off];
+    for (int q = 0; q < A.nfrac; ++q) oq[q] = (rho0 * A.Q[q][off] + dt * kq[q]) / out[0];
+  } else {
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      out[v] = R(0.5) * ((A.U0[v * A.nc + off] + A.Us[v * A.nc + off]) + dt * k[v]);
+    const R rho0 = A.U0[off], rhos = A.Us[off];
+    for (int q = 0; q < A.nfrac; ++q)
+      oq[q] = (R(0.5) * ((rho0 * A.Q0[q][off] + rhos * A.Qs[q][off]) + dt * kq[q])) / out[0];
+  }
+  if (!physical_cell<R, NV>(out)) err |= kMErrNonphysical;
+  const R tol = Exact<R>::value ? R(1e-12) : R(1e-5);
+  for (int q = 0; q < A.nfrac; ++q) {
+    if (oq[q] < -tol || oq[q] > R(1) + tol) err |= kMErrFraction;
+    oq[q] = np_min(np_max(oq[q], R(0)), R(1));  // np.clip
+    A.Qout[q][off] = oq[q];
+  }
+#pragma unroll
+  for (int v = 0; v < NV; ++v) A.Uout[v * A.nc + off] = out[v];
+  return err;
+}
+
+template <typename R, int DIM>
+__global__ void __launch_bounds__(kMThreads) metric_march_update_kernel(MArgs<R> A, int stage) {
+  constexpr int NV = DIM + 2;
+  constexpr int D = DIM - 1;
+  static_assert(DIM >= 2, "1D keeps the separate update");
+  const int chunk = A.chunk;
+  const int n = A.n[D];
+  const int nchunks = (n + chunk - 1) / chunk;  // cells 0..n-1
+  const int64_t ntr = A.nc / n;
+  const int64_t total = ntr * nchunks;
+  const int64_t nfd = A.nf[D];
+  const bool periodic = A.periodic[D];
+  const R dt = R(A.dt);
+  int err = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t tr = t % ntr;
+    const int ch = (int)(t / ntr);
+    MIdx c;
+    c.i = (int)(tr % A.n[0]);
+    if (D == 1) {
+      c.j = 0;
+      c.k = (int)(tr / A.n[0]);
+    } else {
+      c.j = (int)(tr / A.n[0]);
+      c.k = 0;
+    }
+    const int k0 = ch * chunk, k1 = min(k0 + chunk, n);  // cells k0..k1-1, faces k0..k1
+    MCell<R, NV> cl, cr, p;
+    R sl[NV], sr[NV], wlo[NV + 2];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) sl[v] = sr[v] = R(0);
+    err |= padded_cell<R, NV, D>(A, k0, c, cl);
+    err |= padded_cell<R, NV, D>(A, k0 + 1, c, cr);
+    if (!A.first_order) {  // slope of padded cell k0
+      if (k0 >= 1) {
+        MCell<R, NV> m;
+        err |= padded_cell<R, NV, D>(A, k0 - 1, c, m);
+        cell_slope<R, NV>(m, cl, cr, A.limiter, sl);
+      } else if (periodic) {
+        MCell<R, NV> a, b, e;
+        err |= padded_cell<R, NV, D>(A, n - 1, c, a);
+        err |= padded_cell<R, NV, D>(A, n, c, b);
+        err |= padded_cell<R, NV, D>(A, n + 1, c, e);
+        cell_slope<R, NV>(a, b, e, A.limiter, sl);
+      }
+    }
+    for (int f = k0; f <= k1; ++f) {
+      if (f + 2 <= n + 1) err |= padded_cell<R, NV, D>(A, f + 2, c, p);
+      if (!A.first_order) {  // slope of padded cell f + 1
+        if (f + 1 <= n) {
+          cell_slope<R, NV>(cl, cr, p, A.limiter, sr);
+        } else if (periodic) {
+          MCell<R, NV> a, b, e;
+          err |= padded_cell<R, NV, D>(A, 0, c, a);
+          err |= padded_cell<R, NV, D>(A, 1, c, b);
+          err |= padded_cell<R, NV, D>(A, 2, c, e);
+          cell_slope<R, NV>(a, b, e, A.limiter, sr);
+        } else {
+#pragma unroll
+          for (int v = 0; v < NV; ++v) sr[v] = R(0);
+        }
+      }
+      R w[NV + 2];
+      face_flux<R, DIM, D>(A, f, c, cl, cr, sl, sr, w, w + NV);
+      if (f == 0 || f == n) {  // boundary planes: read by the outward sums
+        const int64_t idx = face_off(D, f, c, A.n);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) A.W[D][v * nfd + idx] = w[v];
+      }
+      if (f > k0) {  // cell f - 1: low face in wlo, high face in w
+        MIdx co = c;
+        if (D == 1) co.j = f - 1; else co.k = f - 1;
+        err |= update_cell<R, DIM>(A, co, wlo, w, stage, dt);
+      }
+#pragma unroll
+      for (int v = 0; v < NV + 2; ++v) wlo[v] = w[v];
+      cl = cr;
+      cr = p;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) sl[v] = sr[v];
+    }
   }
   if (err) atomicOr(A.err, err);
 }

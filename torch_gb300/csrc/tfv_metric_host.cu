@@ -189,8 +189,10 @@ struct Driver {
     prim_slot = slot;
     return reduce(slot, g);
   }
-  // one SSPRK2 right-hand side: K, the face fluxes, the source and outward sums
-  int rhs(const View& v, bool first_order, int slot_source, int slot_outward) {
+  // one SSPRK2 right-hand side: K, the face fluxes, the source and outward
+  // sums.  stage > 0 (2D / 3D grids): the last direction's faces are fused
+  // with that stage's update into A.Uout (A.U / A.U0 / A.Us set by the caller)
+  int rhs(const View& v, bool first_order, int slot_source, int slot_outward, int stage = 0) {
     A.first_order = first_order ? 1 : 0;
     if (prim_state == v.u && prim_slot >= 0) {  // primitives of v already computed (dt pass)
       set_input(v);
@@ -201,18 +203,26 @@ struct Driver {
       int r = prim(v, slot_source);
       if (r) return r;
     }
+    const bool fused = stage > 0 && m->dim >= 2;
     for (int d = 0; d < m->dim; ++d) {
-      // x faces: one thread per face; y and z faces: one thread per run of
-      // A.chunk faces, the run as long as keeps eight 256-thread CTAs per SM busy
+      // y and z faces (and the x faces of double-precision 2D / 3D grids): one
+      // thread per run of A.chunk faces (cells, when fused with the update),
+      // the run as long as keeps eight 256-thread CTAs per SM busy; other x
+      // faces: one thread per face
+      const bool last_fused = fused && d == m->dim - 1;
       int64_t work = m->nf[0];
-      if (d > 0) {
-        const int64_t lines = m->nc / m->cfg.n[d], faces = m->cfg.n[d] + 1;
+      if (d > 0 || (m->dim >= 2 && m->esz == 8)) {
+        const int64_t lines = m->nc / m->cfg.n[d];
+        const int64_t runs = m->cfg.n[d] + (last_fused ? 0 : 1);
         const int64_t target = (int64_t)m->sms * 8 * 256;
         A.chunk = (int)std::max<int64_t>(
-            4, std::min<int64_t>(kMChunk, (faces * lines + target - 1) / target));
-        work = lines * ((faces + A.chunk - 1) / A.chunk);
+            4, std::min<int64_t>(kMChunk, (runs * lines + target - 1) / target));
+        work = lines * ((runs + A.chunk - 1) / A.chunk);
       }
-      TFV_MCUDA(launch(kMOpFace, d, grid_for(m, work)));
+      if (last_fused)
+        TFV_MCUDA(launch(kMOpMarchUpdate, stage, grid_for(m, work)));
+      else
+        TFV_MCUDA(launch(kMOpFace, d, grid_for(m, work)));
     }
     int64_t plane = 0;
     for (int d = 0; d < m->dim; ++d) plane = std::max<int64_t>(plane, m->nc / m->cfg.n[d]);
@@ -308,20 +318,25 @@ int metric_step(tfv_metric* m) {
     }
     // SSPRK2, then the same at first order (torchFiniteVolume.py:234-276)
     int used = -1;
+    // single-precision 2D / 3D: the last direction's faces and the stage
+    // update are one kernel (double precision, bound by its FP64 pipe, ran
+    // slower so: it keeps the separate update pass)
+    const bool fused = m->dim >= 2 && m->esz == 4;
     for (int fo = 0; fo < 2 && used < 0; ++fo) {
       TFV_MCUDA(cudaMemsetAsync(D.A.err, 0, sizeof(int32_t), D.s));
-      if ((r = D.rhs(old, fo == 1, kSlotSource1, kSlotOutward1))) return r;
-      D.set_input(old);
       D.A.Uout = (R*)stage.u;
       D.A.Qout[0] = (R*)stage.q[0];
       D.A.Qout[1] = (R*)stage.q[1];
-      TFV_MCUDA(D.launch(kMOpUpdate, 1, grid_for(m, m->nc)));
+      if ((r = D.rhs(old, fo == 1, kSlotSource1, kSlotOutward1, fused ? 1 : 0))) return r;
+      if (!fused) {
+        D.set_input(old);
+        TFV_MCUDA(D.launch(kMOpUpdate, 1, grid_for(m, m->nc)));
+      }
       int32_t e1 = 0;
       TFV_MCUDA(cudaMemcpyAsync(&e1, D.A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, D.s));
       TFV_MCUDA(cudaStreamSynchronize(D.s));
       if ((r = D.boundary_error(e1))) return r;
       if (e1 & (kMErrNonphysical | kMErrFraction)) continue;
-      if ((r = D.rhs(stage, fo == 1, kSlotSource2, kSlotOutward2))) return r;
       D.A.U0 = (const R*)old.u;
       D.A.Q0[0] = (const R*)old.q[0];
       D.A.Q0[1] = (const R*)old.q[1];
@@ -331,7 +346,8 @@ int metric_step(tfv_metric* m) {
       D.A.Uout = (R*)next.u;
       D.A.Qout[0] = (R*)next.q[0];
       D.A.Qout[1] = (R*)next.q[1];
-      TFV_MCUDA(D.launch(kMOpUpdate, 2, grid_for(m, m->nc)));
+      if ((r = D.rhs(stage, fo == 1, kSlotSource2, kSlotOutward2, fused ? 2 : 0))) return r;
+      if (!fused) TFV_MCUDA(D.launch(kMOpUpdate, 2, grid_for(m, m->nc)));
       int32_t e2 = 0;
       TFV_MCUDA(cudaMemcpyAsync(&e2, D.A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, D.s));
       TFV_MCUDA(cudaStreamSynchronize(D.s));

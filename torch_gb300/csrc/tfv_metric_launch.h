@@ -16,6 +16,7 @@ enum : int {
   kMOpRate = 4,      // CFL rate maximum
   kMOpReact = 5,     // arg = 0: reaction half into Uout; 1: closing half in place + source partials
   kMOpIntegral = 6,  // partials of the state integral
+  kMOpMarchUpdate = 7,  // arg = SSPRK2 stage: last-direction faces + update (2D / 3D)
 };
 
 cudaError_t metric_launch_f64(int op, int dim, const MArgs<double>& A, int arg, int grid,
