@@ -268,6 +268,7 @@ __global__ void __launch_bounds__(kMThreads) metric_prim_kernel(MArgs<R> A) {
 #pragma unroll
     for (int v = 0; v < NV; ++v) A.P[v * A.nc + off] = p[v];
     if (A.reactive) A.G[off] = g;
+    A.S[off] = sqrt((g * p[NV - 1]) / p[0]);  // as cell_speed forms it
     R s[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) s[v] = R(0);
@@ -812,29 +813,33 @@ __device__ __forceinline__ R cell_speed(const MCell<R, DIM + 2>& c, int d) {
   return fabs(c.p[d + 1]) + sqrt((c.g * c.p[NV - 1]) / c.p[0]);
 }
 
-// rate of direction D at cell c (self: the cell's primitives)
+// rate of direction D at cell c (self: the cell's primitives, at offset off).
+// The speed |u_D| + a of an interior cell reads a from the sound speeds the
+// primitive pass stored (the same expression as cell_speed); boundary faces
+// build the ghost state and form its speed.
 template <typename R, int DIM, int D>
-__device__ __forceinline__ R direction_rate(const MArgs<R>& A, const MIdx& c,
+__device__ __forceinline__ R direction_rate(const MArgs<R>& A, const MIdx& c, int64_t off,
                                             const MCell<R, DIM + 2>& self, R vol, int& err) {
   constexpr int NV = DIM + 2;
   const int n = A.n[D];
   const int cd = D == 0 ? c.i : (D == 1 ? c.j : c.k);
-  const R s = cell_speed<R, DIM>(self, D);
+  const int64_t stride = D == 0 ? 1 : (D == 1 ? (int64_t)A.n[0] : (int64_t)A.n[0] * A.n[1]);
+  const R s = fabs(self.p[D + 1]) + A.S[off];
   R fs_lo, fs_hi;
   MCell<R, NV> o;
   if (cd == 0) {  // boundary_state of the low face
     err |= padded_cell<R, NV, D>(A, 0, c, o);
     fs_lo = np_max(s, fabs(o.p[D + 1]) + sqrt((o.g * o.p[NV - 1]) / o.p[0]));
-  } else {
-    err |= padded_cell<R, NV, D>(A, cd, c, o);  // interior neighbour below
-    fs_lo = np_max(cell_speed<R, DIM>(o, D), s);
+  } else {  // interior neighbour below
+    const int64_t nb = off - stride;
+    fs_lo = np_max(fabs(A.P[(D + 1) * A.nc + nb]) + A.S[nb], s);
   }
   if (cd == n - 1) {
     err |= padded_cell<R, NV, D>(A, n + 1, c, o);
     fs_hi = np_max(s, fabs(o.p[D + 1]) + sqrt((o.g * o.p[NV - 1]) / o.p[0]));
-  } else {
-    err |= padded_cell<R, NV, D>(A, cd + 2, c, o);  // interior neighbour above
-    fs_hi = np_max(s, cell_speed<R, DIM>(o, D));
+  } else {  // interior neighbour above
+    const int64_t nb = off + stride;
+    fs_hi = np_max(s, fabs(A.P[(D + 1) * A.nc + nb]) + A.S[nb]);
   }
   return np_max(area<R, DIM>(A, D, cd, c) * fs_lo, area<R, DIM>(A, D, cd + 1, c) * fs_hi) / vol;
 }
@@ -851,9 +856,9 @@ __global__ void __launch_bounds__(kMThreads) metric_rate_kernel(MArgs<R> A) {
     const R vol = volume<R, DIM>(A, c);
     MCell<R, NV> self;
     load_cell<R, NV>(A, off, self);
-    R rate = direction_rate<R, DIM, 0>(A, c, self, vol, err);
-    if constexpr (DIM >= 2) rate = rate + direction_rate<R, DIM, 1>(A, c, self, vol, err);
-    if constexpr (DIM == 3) rate = rate + direction_rate<R, DIM, 2>(A, c, self, vol, err);
+    R rate = direction_rate<R, DIM, 0>(A, c, off, self, vol, err);
+    if constexpr (DIM >= 2) rate = rate + direction_rate<R, DIM, 1>(A, c, off, self, vol, err);
+    if constexpr (DIM == 3) rate = rate + direction_rate<R, DIM, 2>(A, c, off, self, vol, err);
     if (!(rate == rate) || isinf(rate)) err |= kMErrRate;
     best = np_max(best, rate);
   }

@@ -83,6 +83,7 @@ struct MArgs {
   // outputs and scratch
   R* P;               // primitives [nv][nc]
   R* G;               // gamma [nc] (reactive)
+  R* S;               // sound speed sqrt(gamma p / rho) [nc] of the primitives in P
   R* K;               // d state / dt [nv][nc]
   R* W[3];            // area-weighted fluxes per direction [nv][nf]
   R* T[3];            // area-weighted fraction transport per direction [nfrac][nf]

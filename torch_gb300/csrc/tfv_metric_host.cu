@@ -43,7 +43,7 @@ struct tfv_metric {
   size_t esz = 8;
   // workspace offsets (bytes)
   size_t off_state_a = 0, off_q_a[2] = {0, 0}, off_state_b = 0, off_q_b[2] = {0, 0};
-  size_t off_p = 0, off_g = 0, off_k = 0, off_w[3] = {0, 0, 0}, off_t[3] = {0, 0, 0};
+  size_t off_p = 0, off_g = 0, off_s = 0, off_k = 0, off_w[3] = {0, 0, 0}, off_t[3] = {0, 0, 0};
   size_t off_faces = 0, off_fac = 0, off_part = 0, off_res = 0, off_rate = 0, off_err = 0, ws_size = 0;
   unsigned char* ws = nullptr;
   void* ring[2] = {nullptr, nullptr};
@@ -129,6 +129,7 @@ MArgs<R> make_args(const tfv_metric* m) {
     }
   A.P = reinterpret_cast<R*>(m->ws + m->off_p);
   A.G = reinterpret_cast<R*>(m->ws + m->off_g);
+  A.S = reinterpret_cast<R*>(m->ws + m->off_s);
   A.K = reinterpret_cast<R*>(m->ws + m->off_k);
   for (int d = 0; d < 3; ++d) {
     A.W[d] = reinterpret_cast<R*>(m->ws + m->off_w[d]);
@@ -494,6 +495,7 @@ int tfv_metric_create(int32_t precision, const tfv_metric_config* cfg, const dou
   m->off_q_b[1] = take(sc);
   m->off_p = take(st);
   m->off_g = take(sc);
+  m->off_s = take(sc);
   m->off_k = take(st);
   for (int d = 0; d < m->dim; ++d) {
     m->off_w[d] = take(m->esz * m->nv * m->nf[d]);
