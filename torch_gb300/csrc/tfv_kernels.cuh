@@ -509,8 +509,16 @@ __device__ __forceinline__ void cell_stage(const R* ringm, const R* ringc, const
       flux2<R>(vp, g, dd, fp);
       flux2<R>(vm, g, dd, fm);
     }
+    if constexpr (!Exact<R>::value && DIM == 3) {
+      // single precision 3D: the mass fluxes are the normal momenta
+      // (flux3), so their difference is the normal momentum's slope
+      ubar[0] = ubar[0] - coefh[dd] * s[dd + 1];
 #pragma unroll
-    for (int c = 0; c < NV; ++c) ubar[c] = ubar[c] - coefh[dd] * (fp[c] - fm[c]);
+      for (int c = 1; c < NV; ++c) ubar[c] = ubar[c] - coefh[dd] * (fp[c] - fm[c]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < NV; ++c) ubar[c] = ubar[c] - coefh[dd] * (fp[c] - fm[c]);
+    }
     if (dd == 0) {
 #pragma unroll
       for (int c = 0; c < NV; ++c) bsa[c * bplane + bi] = s[c];

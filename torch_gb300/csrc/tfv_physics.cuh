@@ -44,6 +44,14 @@ __device__ __forceinline__ float np_min(float a, float b) {
   return r;
 }
 
+// numpy.maximum(a, numpy.maximum(b, c)) in one instruction: NaN if any
+// operand is NaN (three-operand max, sm_100 and later).
+__device__ __forceinline__ float np_max3(float a, float b, float c) {
+  float r;
+  asm("max.NaN.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 // a / b: IEEE division (double) or the approximate single-precision one.
 __device__ __forceinline__ double dv(double a, double b) { return a / b; }
 __device__ __forceinline__ float dv(float a, float b) { return __fdividef(a, b); }
@@ -89,7 +97,7 @@ __device__ __forceinline__ R limited_slope(R um, R uc, R up) {
     if (LIM == 2)
       t = np_max(R(0), np_min(a, b));
     else
-      t = np_max(R(0), np_max(np_min(a + a, b), np_min(a, b + b)));
+      t = np_max3(R(0), np_min(a + a, b), np_min(a, b + b));
     return t * s;
   }
   if constexpr (!Exact<R>::value && LIM == 0) {
@@ -147,6 +155,7 @@ __device__ __forceinline__ void flux3(const R* u, R g, int m, R* f) {
   }
 #pragma unroll
   for (int c = 0; c < 4; ++c) f[c] = u[c] * vel;
+  if constexpr (!Exact<R>::value) f[0] = u[m];  // rho * (m / rho) is the momentum itself
   f[m] = f[m] + p;
   f[4] = vel * (u[4] + p);
 }
@@ -345,8 +354,11 @@ __device__ __forceinline__ void hllc_gated(const float* ul, const float* ur, flo
   constexpr int E = NV - 1;
   const float fl = float(kFloor);
   const float g = 0.5f * (gl + gr);
-  const float rl = np_max(ul[0], fl);
-  const float rr = np_max(ur[0], fl);
+  // the density floors of the reference change nothing here: a face state
+  // whose density is not above the floor fails the gate test below and the
+  // step is redone to first order
+  const float rl = ul[0];
+  const float rr = ur[0];
   const float irl = rcp(rl), irr = rcp(rr);
   const float unl = ul[1] * irl, unr = ur[1] * irr;
   float utl[NT], utr[NT];
@@ -422,9 +434,12 @@ __device__ __forceinline__ void hllc_gated(const float* ul, const float* ur, flo
 #pragma unroll
     for (int c = 0; c < NV; ++c) f[c] = f[c] + s * (star[c] - u[c]);
   }
-  const bool any = mr || mstar || ml;
+  // No NaN select for "no region": with face states that pass the gate test
+  // above, sL, sR and ss are finite and one of the three regions always
+  // holds; states that fail it flag the tile, and the flagged step is redone
+  // to first order, so this flux is never committed.
 #pragma unroll
-  for (int c = 0; c < NV; ++c) out[c] = any ? f[c] : NAN;
+  for (int c = 0; c < NV; ++c) out[c] = f[c];
 }
 
 template <int NV>
