@@ -48,6 +48,24 @@ __device__ __forceinline__ MIdx cell_of(int64_t off, const int* n) {
   c.k = (int)(r / n[1]);
   return c;
 }
+__device__ __forceinline__ uint32_t udiv(uint32_t n, const UDiv& v) {
+  return (uint32_t)(((uint64_t)__umulhi(n, v.m) + n) >> v.l);
+}
+// (x, y) of index r = y * d + x, 0 <= x < d, by the invariant divisor of d
+__device__ __forceinline__ void split32(uint32_t r, const UDiv& v, int& x, int& y) {
+  const uint32_t q = udiv(r, v);
+  x = (int)(r - q * v.d);
+  y = (int)q;
+}
+template <typename R>
+__device__ __forceinline__ MIdx cell_of(int64_t off, const MArgs<R>& A) {
+  if (!A.idx32) return cell_of(off, A.n);
+  MIdx c;
+  int r;
+  split32((uint32_t)off, A.dn0, c.i, r);
+  split32((uint32_t)r, A.dn1, c.j, c.k);
+  return c;
+}
 __device__ __forceinline__ int64_t off_of(int i, int j, int k, const int* n) {
   return ((int64_t)k * n[1] + j) * n[0] + i;
 }
@@ -273,7 +291,7 @@ __global__ void __launch_bounds__(kMThreads) metric_prim_kernel(MArgs<R> A) {
 #pragma unroll
     for (int v = 0; v < NV; ++v) s[v] = R(0);
     if (A.geometry != kGeoCartesian) {  // torchGeometry.py:177-204
-      const MIdx c = cell_of(off, A.n);
+      const MIdx c = cell_of(off, A);
       const R vol = volume<R, DIM>(A, c);
       const R rho = p[0], pr = p[NV - 1];
       const R radial = (area<R, DIM>(A, 0, c.i + 1, c) - area<R, DIM>(A, 0, c.i, c)) / vol;
@@ -412,7 +430,22 @@ __global__ void __launch_bounds__(kMThreads) metric_face_kernel(MArgs<R> A) {
     // face coordinates: f along d, the cell counts along the others
     MIdx c;
     int f;
-    if (d == 0) {
+    if (A.idx32) {
+      int r;
+      if (d == 0) {
+        split32((uint32_t)idx, A.dn0f, f, r);
+        split32((uint32_t)r, A.dn1, c.j, c.k);
+        c.i = 0;
+      } else if (d == 1) {
+        split32((uint32_t)idx, A.dn0, c.i, r);
+        split32((uint32_t)r, A.dn1f, f, c.k);
+        c.j = 0;
+      } else {
+        split32((uint32_t)idx, A.dn0, c.i, r);
+        split32((uint32_t)r, A.dn1, c.j, f);
+        c.k = 0;
+      }
+    } else if (d == 0) {
       f = (int)(idx % (n + 1));
       const int64_t r = idx / (n + 1);
       c.j = (int)(r % A.n[1]);
@@ -568,7 +601,7 @@ __global__ void __launch_bounds__(kMThreads) metric_update_kernel(MArgs<R> A, in
   const R dt = R(A.dt);
   for (int64_t off = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; off < A.nc;
        off += (int64_t)gridDim.x * blockDim.x) {
-    const MIdx c = cell_of(off, A.n);
+    const MIdx c = cell_of(off, A);
     const R vol = volume<R, DIM>(A, c);
     R k[NV], kq[2] = {R(0), R(0)};
 #pragma unroll
@@ -852,7 +885,7 @@ __global__ void __launch_bounds__(kMThreads) metric_rate_kernel(MArgs<R> A) {
   int err = 0;
   for (int64_t off = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; off < A.nc;
        off += (int64_t)gridDim.x * blockDim.x) {
-    const MIdx c = cell_of(off, A.n);
+    const MIdx c = cell_of(off, A);
     const R vol = volume<R, DIM>(A, c);
     MCell<R, NV> self;
     load_cell<R, NV>(A, off, self);
@@ -897,7 +930,7 @@ __global__ void __launch_bounds__(kMThreads) metric_react_kernel(MArgs<R> A, int
     R beta = znd ? (mode == 0 ? A.Q[1][off] : A.Qout[1][off]) : R(1);
     if (!react_cell<R, DIM>(chem, u, lam, beta, znd, 0.5 * A.dt)) err |= kMErrChemistry;
     if (mode == 1) {
-      const MIdx c = cell_of(off, A.n);
+      const MIdx c = cell_of(off, A);
       const double vol = (double)volume<R, DIM>(A, c);
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
@@ -932,7 +965,7 @@ __global__ void __launch_bounds__(kMThreads) metric_integral_kernel(MArgs<R> A) 
   for (int64_t off = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; off < A.nc;
        off += (int64_t)gridDim.x * blockDim.x) {
     double w = 1.0;
-    if (A.geometry != kGeoCartesian) w = (double)volume<R, DIM>(A, cell_of(off, A.n));
+    if (A.geometry != kGeoCartesian) w = (double)volume<R, DIM>(A, cell_of(off, A));
 #pragma unroll
     for (int v = 0; v < NV; ++v) part[v] += (double)A.U[v * A.nc + off] * w;
   }

@@ -50,6 +50,23 @@ struct MFace {
   R p0, t0, rgas;  // stagnation inlet: total pressure, temperature, gas constant
 };
 
+// Unsigned 32-bit division by an invariant divisor d as a multiply-high, an
+// add and a shift (Granlund and Montgomery, "Division by invariant integers
+// using multiplication", PLDI 1994, unsigned case with N = 32): with
+// l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1, the quotient of
+// every n < 2^32 is (mulhi(m, n) + n) >> l, the sum formed in 64 bits.
+struct UDiv {
+  uint32_t d, m, l;
+};
+inline UDiv make_udiv(uint32_t d) {
+  UDiv v;
+  v.d = d;
+  v.l = 0;
+  while (v.l < 32 && (uint64_t(1) << v.l) < d) ++v.l;
+  v.m = (uint32_t)(((uint64_t(1) << 32) * ((uint64_t(1) << v.l) - d)) / d + 1);
+  return v;
+}
+
 constexpr int kMReduceBlocks = 512;  // fixed block count of every reduction (deterministic)
 constexpr int kMChunk = 32;          // longest run of y / z faces marched by one thread
 
@@ -58,6 +75,10 @@ struct MArgs {
   int32_t n[3];       // cells along x, y, z (1 beyond the active axes)
   int64_t nc;         // cells
   int64_t nf[3];      // faces per direction
+  // cell and face indexes below 2^31: decoded with the invariant divisors
+  // n[0], n[1], n[0] + 1 and n[1] + 1 instead of 64-bit division
+  int32_t idx32;
+  UDiv dn0, dn1, dn0f, dn1f;
   int32_t nfrac;      // transported fractions (0, 1 or 2)
   int32_t reactive;   // gamma from lambda (SI closure)
   int32_t limiter;    // 0 VanLeer, 1 Albada, 2 MINBEE, 3 Superbee, 4 Unos

@@ -99,6 +99,13 @@ MArgs<R> make_args(const tfv_metric* m) {
   for (int a = 0; a < 3; ++a) A.n[a] = a < m->dim ? m->cfg.n[a] : 1;
   A.nc = m->nc;
   for (int d = 0; d < 3; ++d) A.nf[d] = m->nf[d];
+  int64_t top = A.nc;
+  for (int d = 0; d < 3; ++d) top = std::max<int64_t>(top, A.nf[d]);
+  A.idx32 = top < (int64_t(1) << 31);
+  A.dn0 = make_udiv((uint32_t)A.n[0]);
+  A.dn1 = make_udiv((uint32_t)A.n[1]);
+  A.dn0f = make_udiv((uint32_t)A.n[0] + 1);
+  A.dn1f = make_udiv((uint32_t)A.n[1] + 1);
   A.nfrac = m->nfrac;
   A.reactive = m->cfg.reactive;
   A.limiter = m->cfg.limiter;
