@@ -36,6 +36,13 @@ __device__ __forceinline__ double tpow<double>(double a, double b) { return pow(
 template <>
 __device__ __forceinline__ float tpow<float>(float a, float b) { return powf(a, b); }
 
+// Read of an array that no thread of the running kernel writes (the
+// non-coherent load path; lets loads move ahead of the kernel's stores).
+template <typename T>
+__device__ __forceinline__ T ro(const T* p) {
+  return __ldg(p);
+}
+
 // cell coordinates of a linear index
 struct MIdx {
   int i, j, k;
@@ -73,9 +80,9 @@ __device__ __forceinline__ int64_t off_of(int i, int j, int k, const int* n) {
 // volume of cell (i, j, k): factors multiplied x, y, z
 template <typename R, int DIM>
 __device__ __forceinline__ R volume(const MArgs<R>& A, const MIdx& c) {
-  R v = A.vf[0][c.i];
-  if (DIM >= 2) v = v * A.vf[1][c.j];
-  if (DIM == 3) v = v * A.vf[2][c.k];
+  R v = ro(&A.vf[0][c.i]);
+  if (DIM >= 2) v = v * ro(&A.vf[1][c.j]);
+  if (DIM == 3) v = v * ro(&A.vf[2][c.k]);
   return v;
 }
 
@@ -83,9 +90,9 @@ __device__ __forceinline__ R volume(const MArgs<R>& A, const MIdx& c) {
 template <typename R, int DIM>
 __device__ __forceinline__ R area(const MArgs<R>& A, int d, int f, const MIdx& c) {
   const int idx[3] = {d == 0 ? f : c.i, d == 1 ? f : c.j, d == 2 ? f : c.k};
-  R a = A.ff[d][0][idx[0]];
-  if (DIM >= 2) a = a * A.ff[d][1][idx[1]];
-  if (DIM == 3) a = a * A.ff[d][2][idx[2]];
+  R a = ro(&A.ff[d][0][idx[0]]);
+  if (DIM >= 2) a = a * ro(&A.ff[d][1][idx[1]]);
+  if (DIM == 3) a = a * ro(&A.ff[d][2][idx[2]]);
   return a;
 }
 
@@ -124,10 +131,10 @@ struct MCell {
 template <typename R, int NV>
 __device__ __forceinline__ void load_cell(const MArgs<R>& A, int64_t off, MCell<R, NV>& c) {
 #pragma unroll
-  for (int v = 0; v < NV; ++v) c.p[v] = A.P[v * A.nc + off];
-  c.g = A.reactive ? A.G[off] : A.gam;
-  c.q[0] = A.nfrac > 0 ? A.Q[0][off] : R(0);
-  c.q[1] = A.nfrac > 1 ? A.Q[1][off] : R(0);
+  for (int v = 0; v < NV; ++v) c.p[v] = ro(&A.P[v * A.nc + off]);
+  c.g = A.reactive ? ro(&A.G[off]) : A.gam;
+  c.q[0] = A.nfrac > 0 ? ro(&A.Q[0][off]) : R(0);
+  c.q[1] = A.nfrac > 1 ? ro(&A.Q[1][off]) : R(0);
 }
 
 // Boundary state built from the boundary cell (torchBoundaries.py:185-246).
@@ -415,7 +422,8 @@ __device__ __forceinline__ void emit_face(const MArgs<R>& A, int f, const MIdx& 
   face_flux<R, DIM, D>(A, f, c, cl, cr, sl, sr, W, T);
 #pragma unroll
   for (int v = 0; v < NV; ++v) A.W[D][v * nf + idx] = W[v];
-  for (int q = 0; q < A.nfrac; ++q) A.T[D][q * nf + idx] = T[q];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) if (q < A.nfrac) A.T[D][q * nf + idx] = T[q];
 }
 
 template <typename R, int DIM, int D>
@@ -605,37 +613,41 @@ __global__ void __launch_bounds__(kMThreads) metric_update_kernel(MArgs<R> A, in
     const R vol = volume<R, DIM>(A, c);
     R k[NV], kq[2] = {R(0), R(0)};
 #pragma unroll
-    for (int v = 0; v < NV; ++v) k[v] = A.K[v * A.nc + off];
+    for (int v = 0; v < NV; ++v) k[v] = ro(&A.K[v * A.nc + off]);
     const int cc[3] = {c.i, c.j, c.k};
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       const int64_t lo = face_off(d, cc[d], c, A.n), hi = face_off(d, cc[d] + 1, c, A.n);
       const int64_t nf = A.nf[d];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) k[v] = k[v] - (A.W[d][v * nf + hi] - A.W[d][v * nf + lo]) / vol;
-      for (int q = 0; q < A.nfrac; ++q)
-        kq[q] = kq[q] - (A.T[d][q * nf + hi] - A.T[d][q * nf + lo]) / vol;
+      for (int v = 0; v < NV; ++v) k[v] = k[v] - (ro(&A.W[d][v * nf + hi]) - ro(&A.W[d][v * nf + lo])) / vol;
+#pragma unroll
+      for (int q = 0; q < 2; ++q) if (q < A.nfrac)
+        kq[q] = kq[q] - (ro(&A.T[d][q * nf + hi]) - ro(&A.T[d][q * nf + lo])) / vol;
     }
     R out[NV], oq[2];
     if (stage == 1) {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) out[v] = A.U[v * A.nc + off] + dt * k[v];
-      const R rho0 = A.U[off];
-      for (int q = 0; q < A.nfrac; ++q)
-        oq[q] = (rho0 * A.Q[q][off] + dt * kq[q]) / out[0];
+      for (int v = 0; v < NV; ++v) out[v] = ro(&A.U[v * A.nc + off]) + dt * k[v];
+      const R rho0 = ro(&A.U[off]);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) if (q < A.nfrac)
+        oq[q] = (rho0 * ro(&A.Q[q][off]) + dt * kq[q]) / out[0];
     } else {
 #pragma unroll
       for (int v = 0; v < NV; ++v)
-        out[v] = R(0.5) * ((A.U0[v * A.nc + off] + A.Us[v * A.nc + off]) + dt * k[v]);
-      const R rho0 = A.U0[off], rhos = A.Us[off];
-      for (int q = 0; q < A.nfrac; ++q)
-        oq[q] = (R(0.5) * ((rho0 * A.Q0[q][off] + rhos * A.Qs[q][off]) + dt * kq[q])) / out[0];
+        out[v] = R(0.5) * ((ro(&A.U0[v * A.nc + off]) + ro(&A.Us[v * A.nc + off])) + dt * k[v]);
+      const R rho0 = ro(&A.U0[off]), rhos = ro(&A.Us[off]);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) if (q < A.nfrac)
+        oq[q] = (R(0.5) * ((rho0 * ro(&A.Q0[q][off]) + rhos * ro(&A.Qs[q][off])) + dt * kq[q])) / out[0];
     }
     if (!physical_cell<R, NV>(out)) err |= kMErrNonphysical;
     // the reference's interval check (1e-12); single-precision roundoff of a
     // fraction of exactly 1 needs a wider margin
     const R tol = Exact<R>::value ? R(1e-12) : R(1e-5);
-    for (int q = 0; q < A.nfrac; ++q) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) if (q < A.nfrac) {
       if (oq[q] < -tol || oq[q] > R(1) + tol) err |= kMErrFraction;
       oq[q] = np_min(np_max(oq[q], R(0)), R(1));  // np.clip
       A.Qout[q][off] = oq[q];
@@ -666,40 +678,45 @@ __device__ __forceinline__ int update_cell(const MArgs<R>& A, const MIdx& co, co
   const R vol = volume<R, DIM>(A, co);
   R k[NV], kq[2] = {R(0), R(0)};
 #pragma unroll
-  for (int v = 0; v < NV; ++v) k[v] = A.K[v * A.nc + off];
+  for (int v = 0; v < NV; ++v) k[v] = ro(&A.K[v * A.nc + off]);
   const int cc[3] = {co.i, co.j, co.k};
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     if (d == D) {
 #pragma unroll
       for (int v = 0; v < NV; ++v) k[v] = k[v] - (whi[v] - wlo[v]) / vol;
-      for (int q = 0; q < A.nfrac; ++q) kq[q] = kq[q] - (whi[NV + q] - wlo[NV + q]) / vol;
+#pragma unroll
+      for (int q = 0; q < 2; ++q) if (q < A.nfrac) kq[q] = kq[q] - (whi[NV + q] - wlo[NV + q]) / vol;
     } else {
       const int64_t lo = face_off(d, cc[d], co, A.n), hi = face_off(d, cc[d] + 1, co, A.n);
       const int64_t nf = A.nf[d];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) k[v] = k[v] - (A.W[d][v * nf + hi] - A.W[d][v * nf + lo]) / vol;
-      for (int q = 0; q < A.nfrac; ++q)
-        kq[q] = kq[q] - (A.T[d][q * nf + hi] - A.T[d][q * nf + lo]) / vol;
+      for (int v = 0; v < NV; ++v) k[v] = k[v] - (ro(&A.W[d][v * nf + hi]) - ro(&A.W[d][v * nf + lo])) / vol;
+#pragma unroll
+      for (int q = 0; q < 2; ++q) if (q < A.nfrac)
+        kq[q] = kq[q] - (ro(&A.T[d][q * nf + hi]) - ro(&A.T[d][q * nf + lo])) / vol;
     }
   }
   R out[NV], oq[2];
   if (stage == 1) {
 #pragma unroll
-    for (int v = 0; v < NV; ++v) out[v] = A.U[v * A.nc + off] + dt * k[v];
-    const R rho0 = A.U[off];
-    for (int q = 0; q < A.nfrac; ++q) oq[q] = (rho0 * A.Q[q][off] + dt * kq[q]) / out[0];
+    for (int v = 0; v < NV; ++v) out[v] = ro(&A.U[v * A.nc + off]) + dt * k[v];
+    const R rho0 = ro(&A.U[off]);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) if (q < A.nfrac) oq[q] = (rho0 * ro(&A.Q[q][off]) + dt * kq[q]) / out[0];
   } else {
 #pragma unroll
     for (int v = 0; v < NV; ++v)
-      out[v] = R(0.5) * ((A.U0[v * A.nc + off] + A.Us[v * A.nc + off]) + dt * k[v]);
-    const R rho0 = A.U0[off], rhos = A.Us[off];
-    for (int q = 0; q < A.nfrac; ++q)
-      oq[q] = (R(0.5) * ((rho0 * A.Q0[q][off] + rhos * A.Qs[q][off]) + dt * kq[q])) / out[0];
+      out[v] = R(0.5) * ((ro(&A.U0[v * A.nc + off]) + ro(&A.Us[v * A.nc + off])) + dt * k[v]);
+    const R rho0 = ro(&A.U0[off]), rhos = ro(&A.Us[off]);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) if (q < A.nfrac)
+      oq[q] = (R(0.5) * ((rho0 * ro(&A.Q0[q][off]) + rhos * ro(&A.Qs[q][off])) + dt * kq[q])) / out[0];
   }
   if (!physical_cell<R, NV>(out)) err |= kMErrNonphysical;
   const R tol = Exact<R>::value ? R(1e-12) : R(1e-5);
-  for (int q = 0; q < A.nfrac; ++q) {
+#pragma unroll
+  for (int q = 0; q < 2; ++q) if (q < A.nfrac) {
     if (oq[q] < -tol || oq[q] > R(1) + tol) err |= kMErrFraction;
     oq[q] = np_min(np_max(oq[q], R(0)), R(1));  // np.clip
     A.Qout[q][off] = oq[q];
@@ -857,7 +874,7 @@ __device__ __forceinline__ R direction_rate(const MArgs<R>& A, const MIdx& c, in
   const int n = A.n[D];
   const int cd = D == 0 ? c.i : (D == 1 ? c.j : c.k);
   const int64_t stride = D == 0 ? 1 : (D == 1 ? (int64_t)A.n[0] : (int64_t)A.n[0] * A.n[1]);
-  const R s = fabs(self.p[D + 1]) + A.S[off];
+  const R s = fabs(self.p[D + 1]) + ro(&A.S[off]);
   R fs_lo, fs_hi;
   MCell<R, NV> o;
   if (cd == 0) {  // boundary_state of the low face
@@ -865,14 +882,14 @@ __device__ __forceinline__ R direction_rate(const MArgs<R>& A, const MIdx& c, in
     fs_lo = np_max(s, fabs(o.p[D + 1]) + sqrt((o.g * o.p[NV - 1]) / o.p[0]));
   } else {  // interior neighbour below
     const int64_t nb = off - stride;
-    fs_lo = np_max(fabs(A.P[(D + 1) * A.nc + nb]) + A.S[nb], s);
+    fs_lo = np_max(fabs(ro(&A.P[(D + 1) * A.nc + nb])) + ro(&A.S[nb]), s);
   }
   if (cd == n - 1) {
     err |= padded_cell<R, NV, D>(A, n + 1, c, o);
     fs_hi = np_max(s, fabs(o.p[D + 1]) + sqrt((o.g * o.p[NV - 1]) / o.p[0]));
   } else {  // interior neighbour above
     const int64_t nb = off + stride;
-    fs_hi = np_max(s, fabs(A.P[(D + 1) * A.nc + nb]) + A.S[nb]);
+    fs_hi = np_max(s, fabs(ro(&A.P[(D + 1) * A.nc + nb])) + ro(&A.S[nb]));
   }
   return np_max(area<R, DIM>(A, D, cd, c) * fs_lo, area<R, DIM>(A, D, cd + 1, c) * fs_hi) / vol;
 }
