@@ -29,6 +29,16 @@ namespace tfv {
 
 constexpr int kMThreads = 256;
 
+// Launch bounds of the column-marching kernels: the single-precision unit
+// asks for three resident CTAs per SM (80 registers a thread: 24 warps
+// instead of 16 hide the marching loads' latency); double precision leaves
+// the register count to the compiler.
+#if defined(TFV_MARCH_MIN_BLOCKS) && TFV_MARCH_MIN_BLOCKS > 0
+#define TFV_MARCH_BOUNDS __launch_bounds__(kMThreads, TFV_MARCH_MIN_BLOCKS)
+#else
+#define TFV_MARCH_BOUNDS __launch_bounds__(kMThreads)
+#endif
+
 template <typename R>
 __device__ __forceinline__ R tpow(R a, R b);
 template <>
@@ -524,7 +534,7 @@ __device__ __forceinline__ int64_t face_off(int d, int f, const MIdx& c, const i
 // costs one new cell load, one slope and one flux.  The values are those of
 // metric_face_kernel.
 template <typename R, int DIM, int D>
-__global__ void __launch_bounds__(kMThreads) metric_face_march_kernel(MArgs<R> A) {
+__global__ void TFV_MARCH_BOUNDS metric_face_march_kernel(MArgs<R> A) {
   const int chunk = A.chunk;
   constexpr int NV = DIM + 2;
   const int n = A.n[D];
@@ -727,7 +737,7 @@ __device__ __forceinline__ int update_cell(const MArgs<R>& A, const MIdx& co, co
 }
 
 template <typename R, int DIM>
-__global__ void __launch_bounds__(kMThreads) metric_march_update_kernel(MArgs<R> A, int stage) {
+__global__ void TFV_MARCH_BOUNDS metric_march_update_kernel(MArgs<R> A, int stage) {
   constexpr int NV = DIM + 2;
   constexpr int D = DIM - 1;
   static_assert(DIM >= 2, "1D keeps the separate update");
