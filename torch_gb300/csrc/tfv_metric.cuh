@@ -38,6 +38,12 @@ constexpr int kMThreads = 256;
 #else
 #define TFV_MARCH_BOUNDS __launch_bounds__(kMThreads)
 #endif
+// The same for the one-thread-per-face kernel (x faces in single precision).
+#if defined(TFV_FACE_MIN_BLOCKS) && TFV_FACE_MIN_BLOCKS > 0
+#define TFV_FACE_BOUNDS __launch_bounds__(kMThreads, TFV_FACE_MIN_BLOCKS)
+#else
+#define TFV_FACE_BOUNDS __launch_bounds__(kMThreads)
+#endif
 
 template <typename R>
 __device__ __forceinline__ R tpow(R a, R b);
@@ -437,7 +443,7 @@ __device__ __forceinline__ void emit_face(const MArgs<R>& A, int f, const MIdx& 
 }
 
 template <typename R, int DIM, int D>
-__global__ void __launch_bounds__(kMThreads) metric_face_kernel(MArgs<R> A) {
+__global__ void TFV_FACE_BOUNDS metric_face_kernel(MArgs<R> A) {
   constexpr int NV = DIM + 2;
   constexpr int d = D;
   const int n = A.n[d];
@@ -1050,11 +1056,19 @@ __global__ void __launch_bounds__(kMThreads) rusanov_faces_kernel(
 
 // -- 9. block partials -> totals, in block order -------------------------------
 namespace {
-__global__ void metric_reduce_kernel(const double* part, int nblocks, int nv, double* out) {
+__global__ void __launch_bounds__(256) metric_reduce_kernel(const double* part, int nblocks,
+                                                            int nv, double* out) {
+  // the whole CTA stages the partials in shared memory (independent,
+  // coalesced loads), then one thread per component sums them in block
+  // order, the order of a plain sequential sum
+  __shared__ double sp[kMReduceBlocks * 8];
+  const int nb = min(nblocks, kMReduceBlocks);
+  for (int e = threadIdx.x; e < nb * 8; e += blockDim.x) sp[e] = part[e];
+  __syncthreads();
   const int v = threadIdx.x;
   if (v >= nv) return;
   double s = 0.0;
-  for (int b = 0; b < nblocks; ++b) s += part[b * 8 + v];
+  for (int b = 0; b < nb; ++b) s += sp[b * 8 + v];
   out[v] = s;
 }
 }  // namespace

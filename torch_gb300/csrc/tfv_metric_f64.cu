@@ -7,7 +7,7 @@
 
 namespace tfv {
 cudaError_t metric_reduce(const double* part, int nblocks, int nv, double* out, cudaStream_t s) {
-  metric_reduce_kernel<<<1, 32, 0, s>>>(part, nblocks, nv, out);
+  metric_reduce_kernel<<<1, 256, 0, s>>>(part, nblocks, nv, out);
   return cudaGetLastError();
 }
 }  // namespace tfv
