@@ -299,12 +299,11 @@ __global__ void __launch_bounds__(kMThreads) metric_prim_kernel(MArgs<R> A) {
     part[v] = 0.0;
     ksum[v] = kcomp[v] = R(0);
   }
-  for (int64_t off = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; off < A.nc;
-       off += (int64_t)gridDim.x * blockDim.x) {
-    R u[NV], p[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) u[v] = A.U[v * A.nc + off];
-    const R g = A.reactive ? gamma_of_lambda(A.Q[0][off]) : A.gam;
+  // two cells of the thread's grid-stride sequence per iteration, both
+  // loaded before either is processed (twice the loads in flight); they are
+  // processed, and their source summed, in sequence order
+  auto cell = [&](int64_t off, const R* u, R g) {
+    R p[NV];
     primitive_of<R, NV>(u, g, p);
 #pragma unroll
     for (int v = 0; v < NV; ++v) A.P[v * A.nc + off] = p[v];
@@ -351,6 +350,22 @@ __global__ void __launch_bounds__(kMThreads) metric_prim_kernel(MArgs<R> A) {
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) A.K[v * A.nc + off] = s[v];
+  };
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t off = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; off < A.nc;
+       off += 2 * stride) {
+    const int64_t off2 = off + stride;
+    const bool two = off2 < A.nc;
+    R u1[NV], u2[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      u1[v] = ro(&A.U[v * A.nc + off]);
+      u2[v] = two ? ro(&A.U[v * A.nc + off2]) : R(1);
+    }
+    const R g1 = A.reactive ? gamma_of_lambda(ro(&A.Q[0][off])) : A.gam;
+    const R g2 = A.reactive && two ? gamma_of_lambda(ro(&A.Q[0][off2])) : A.gam;
+    cell(off, u1, g1);
+    if (two) cell(off2, u2, g2);
   }
   if constexpr (!Exact<R>::value) {
 #pragma unroll

@@ -244,7 +244,9 @@ struct Driver {
     TFV_MCUDA(cudaMemsetAsync(A.err, 0, sizeof(int32_t), s));
     int r = prim(v, kSlotIntegral);
     if (r) return r;
-    TFV_MCUDA(launch(kMOpRate, 0, reduce_grid(m->nc)));
+    // the rate's block maxima combine by an atomic max (order-free), so its
+    // grid is sized for occupancy, not for the fixed reduction partition
+    TFV_MCUDA(launch(kMOpRate, 0, grid_for(m, m->nc)));
     unsigned long long bits = 0;
     TFV_MCUDA(cudaMemcpyAsync(&bits, A.rate_max, sizeof(bits), cudaMemcpyDeviceToHost, s));
     TFV_MCUDA(cudaMemcpyAsync(err, A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
