@@ -566,20 +566,28 @@ __global__ void TFV_MARCH_BOUNDS metric_face_march_kernel(MArgs<R> A) {
   int err = 0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t tr = t % ntr;
-    const int ch = (int)(t / ntr);
+    int ch;
     MIdx c;
-    c.i = (int)(tr % A.n[0]);
-    if (D == 0) {  // threads adjacent along y; each marches its own row
+    if (D == 0 && A.xlanes) {  // threads adjacent along x: consecutive runs of a row
+      int r;
+      split32((uint32_t)t, A.dnch, ch, r);
+      split32((uint32_t)r, A.dn1, c.j, c.k);
       c.i = 0;
-      c.j = (int)(tr % A.n[1]);
-      c.k = (int)(tr / A.n[1]);
-    } else if (D == 1) {
-      c.j = 0;
-      c.k = (int)(tr / A.n[0]);
     } else {
-      c.j = (int)(tr / A.n[0]);
-      c.k = 0;
+      const int64_t tr = t % ntr;
+      ch = (int)(t / ntr);
+      c.i = (int)(tr % A.n[0]);
+      if (D == 0) {  // threads adjacent along y; each marches its own row
+        c.i = 0;
+        c.j = (int)(tr % A.n[1]);
+        c.k = (int)(tr / A.n[1]);
+      } else if (D == 1) {
+        c.j = 0;
+        c.k = (int)(tr / A.n[0]);
+      } else {
+        c.j = (int)(tr / A.n[0]);
+        c.k = 0;
+      }
     }
     const int f0 = ch * chunk;
     const int f1 = min(f0 + chunk, n + 1);

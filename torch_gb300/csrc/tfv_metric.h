@@ -69,6 +69,7 @@ inline UDiv make_udiv(uint32_t d) {
 
 constexpr int kMReduceBlocks = 512;  // fixed block count of every reduction (deterministic)
 constexpr int kMChunk = 32;          // longest run of y / z faces marched by one thread
+constexpr int kMXRun = 4;            // x faces per thread in the single-precision x march
 
 template <typename R>
 struct MArgs {
@@ -79,6 +80,10 @@ struct MArgs {
   // n[0], n[1], n[0] + 1 and n[1] + 1 instead of 64-bit division
   int32_t idx32;
   UDiv dn0, dn1, dn0f, dn1f;
+  // x faces marched in short runs by threads adjacent along x (run index
+  // fastest, dnch its count per row); 0: threads adjacent along y
+  int32_t xlanes;
+  UDiv dnch;
   int32_t nfrac;      // transported fractions (0, 1 or 2)
   int32_t reactive;   // gamma from lambda (SI closure)
   int32_t limiter;    // 0 VanLeer, 1 Albada, 2 MINBEE, 3 Superbee, 4 Unos

@@ -219,7 +219,16 @@ struct Driver {
       // faces: one thread per face
       const bool last_fused = fused && d == m->dim - 1;
       int64_t work = m->nf[0];
-      if (d > 0 || (m->dim >= 2 && m->esz == 8)) {
+      A.xlanes = 0;
+      if (d == 0 && m->dim >= 2 && m->esz == 4 && A.idx32) {
+        // single-precision x faces: runs of kMXRun faces, threads adjacent
+        // along x (their loads stay within a few lines of one row)
+        A.chunk = kMXRun;
+        const int nchunks = (m->cfg.n[0] + kMXRun) / kMXRun;  // faces 0..n
+        A.dnch = make_udiv((uint32_t)nchunks);
+        A.xlanes = 1;
+        work = (m->nc / m->cfg.n[0]) * nchunks;
+      } else if (d > 0 || (m->dim >= 2 && m->esz == 8)) {
         const int64_t lines = m->nc / m->cfg.n[d];
         const int64_t runs = m->cfg.n[d] + (last_fused ? 0 : 1);
         const int64_t target = (int64_t)m->sms * 8 * 256;
