@@ -341,8 +341,13 @@ int metric_step(tfv_metric* m) {
     // update are one kernel (double precision, bound by its FP64 pipe, ran
     // slower so: it keeps the separate update pass)
     const bool fused = m->dim >= 2 && m->esz == 4;
+    // Both stages are enqueued before the host looks at either: stage 2
+    // reports into its own error word, and when stage 1 failed (checked
+    // first, as the reference orders it) the stage-2 results are discarded.
+    int32_t* const err1 = D.A.err;
     for (int fo = 0; fo < 2 && used < 0; ++fo) {
-      TFV_MCUDA(cudaMemsetAsync(D.A.err, 0, sizeof(int32_t), D.s));
+      TFV_MCUDA(cudaMemsetAsync(err1, 0, 2 * sizeof(int32_t), D.s));
+      D.A.err = err1;
       D.A.Uout = (R*)stage.u;
       D.A.Qout[0] = (R*)stage.q[0];
       D.A.Qout[1] = (R*)stage.q[1];
@@ -351,11 +356,7 @@ int metric_step(tfv_metric* m) {
         D.set_input(old);
         TFV_MCUDA(D.launch(kMOpUpdate, 1, grid_for(m, m->nc)));
       }
-      int32_t e1 = 0;
-      TFV_MCUDA(cudaMemcpyAsync(&e1, D.A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, D.s));
-      TFV_MCUDA(cudaStreamSynchronize(D.s));
-      if ((r = D.boundary_error(e1))) return r;
-      if (e1 & (kMErrNonphysical | kMErrFraction)) continue;
+      D.A.err = err1 + 1;
       D.A.U0 = (const R*)old.u;
       D.A.Q0[0] = (const R*)old.q[0];
       D.A.Q0[1] = (const R*)old.q[1];
@@ -365,13 +366,22 @@ int metric_step(tfv_metric* m) {
       D.A.Uout = (R*)next.u;
       D.A.Qout[0] = (R*)next.q[0];
       D.A.Qout[1] = (R*)next.q[1];
-      if ((r = D.rhs(stage, fo == 1, kSlotSource2, kSlotOutward2, fused ? 2 : 0))) return r;
-      if (!fused) TFV_MCUDA(D.launch(kMOpUpdate, 2, grid_for(m, m->nc)));
-      int32_t e2 = 0;
-      TFV_MCUDA(cudaMemcpyAsync(&e2, D.A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, D.s));
+      const int r2 = D.rhs(stage, fo == 1, kSlotSource2, kSlotOutward2, fused ? 2 : 0);
+      D.A.err = err1;
+      if (r2) return r2;
+      if (!fused) {
+        D.A.err = err1 + 1;
+        const cudaError_t e = D.launch(kMOpUpdate, 2, grid_for(m, m->nc));
+        D.A.err = err1;
+        TFV_MCUDA(e);
+      }
+      int32_t e12[2] = {0, 0};
+      TFV_MCUDA(cudaMemcpyAsync(e12, err1, sizeof(e12), cudaMemcpyDeviceToHost, D.s));
       TFV_MCUDA(cudaStreamSynchronize(D.s));
-      if ((r = D.boundary_error(e2))) return r;
-      if (e2 & (kMErrNonphysical | kMErrFraction)) continue;
+      if ((r = D.boundary_error(e12[0]))) return r;
+      if (e12[0] & (kMErrNonphysical | kMErrFraction)) continue;
+      if ((r = D.boundary_error(e12[1]))) return r;
+      if (e12[1] & (kMErrNonphysical | kMErrFraction)) continue;
       used = fo;
     }
     if (used < 0) {  // lost positivity at both orders: halve dt
@@ -524,7 +534,7 @@ int tfv_metric_create(int32_t precision, const tfv_metric_config* cfg, const dou
   m->off_part = take(sizeof(double) * kMReduceBlocks * 8);
   m->off_res = take(sizeof(double) * kSlots * 8);
   m->off_rate = take(sizeof(unsigned long long));
-  m->off_err = take(sizeof(int32_t));
+  m->off_err = take(2 * sizeof(int32_t));  // error words of the two SSPRK2 stages
   m->ws_size = o;
   *out = m;
   return TFV_OK;
