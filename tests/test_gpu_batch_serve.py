@@ -145,12 +145,14 @@ def blocks3(shape, seed):
 
 
 @pytest.mark.parametrize("tile", [(16, 12, 40), (16, 12, 7), (32, 8, 40), (24, 8, 16),
-                                  (16, 6, 40)])
+                                  (16, 6, 40), (12, 12, 40), (12, 10, 20)])
 def test_fp32_3d_state_independent_of_tile_shape(tile):
     """The cell arithmetic does not depend on how cells are dealt to threads:
     the fixed-shape 16x16 and 32x8 kernels, the runtime-shape kernel (16x12,
-    24x8, 16x6) and short chunks give the same FP32 state after 12 steps on a
-    grid with partial tiles in x and y, for three limiters."""
+    24x8, 16x6), tiles whose ring cells run on lanes after the owners (12x12,
+    12x10: not whole warps of cells) and short chunks give the same FP32
+    state after 12 steps on a grid with partial tiles in x and y, for three
+    limiters."""
     shape = (37, 45, 70)
     lims = ("MINBEE", "Superbee", "VanLeer")
 
@@ -164,6 +166,33 @@ def test_fp32_3d_state_independent_of_tile_shape(tile):
         return gs
 
     ref = run((16, 16, 40))
+    got = run(tile)
+    for g, h in zip(got, ref):
+        assert g.steps == h.steps == 12
+        assert g.time == h.time
+        np.testing.assert_array_equal(g.state_host(), h.state_host())
+
+
+@pytest.mark.parametrize("tile", [(124, 1, 32), (124, 1, 7), (100, 1, 16), (252, 1, 16),
+                                  (96, 1, 16), (256, 1, 32)])
+def test_fp32_2d_state_independent_of_tile_shape(tile):
+    """2D: 128-cell rows (the reference tile here), rows of 124 and 100 cells
+    whose two ring cells run on the lanes after the owners, 252 (no tensor
+    copies: the box would exceed 256), 96 and 256 give the same FP32 state
+    after 12 steps on grids with partial rows, for three limiters."""
+    sizes = (250, 190, 131)
+    lims = ("MINBEE", "Superbee", "VanLeer")
+
+    def run(t):
+        gs = [Grid(quadrant(n, 21 + k), [1, 1], precision="fp32", t_end=1.0, limiter=lim)
+              for k, (n, lim) in enumerate(zip(sizes, lims))]
+        b = Batch(gs, tile=t)
+        b.advance(12)
+        b.refresh()
+        b.close()
+        return gs
+
+    ref = run((128, 1, 32))
     got = run(tile)
     for g, h in zip(got, ref):
         assert g.steps == h.steps == 12

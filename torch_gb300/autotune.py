@@ -30,7 +30,9 @@ def candidates(dim, precision, sms):
             for chunk in (16, 32, 40, 64):
                 out.append((tx, ty, chunk, 0, 1))
     elif dim == 2:
-        for tx in (128, 256):
+        # 124: rows of 124 cells whose two ring cells take the lanes after the
+        # owners (single precision only: double precision tiles are whole warps)
+        for tx in ((124, 128, 256) if precision == "fp32" else (128, 256)):
             for chunk in (16, 32, 64):
                 for pers in (0, 2 * sms):
                     out.append((tx, 1, chunk, pers, 1))

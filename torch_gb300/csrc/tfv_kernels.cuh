@@ -315,12 +315,13 @@ struct HydroSmem {
   // x offset of cell a = 0 in a staged row: a tensor-copy box must start on a
   // 16-byte boundary, so the row holds 16 bytes of halo on each side.
   static constexpr int kXo = 16 / (int)sizeof(R);
-  int tx, ty, pw, ph, bw, bh, xo;
+  int tx, ty, pw, ph, bw, bh, xo, nthreads;
   size_t slot_elems;  // elements per ring slot (128-byte multiple)
   size_t ring_off, bar_off, box_off, fa_off, fb_off, bs_off, red_off, items_off, bytes;
   __host__ __device__ void init(int tx_, int ty_) {
     tx = tx_;
     ty = DIM == 3 ? ty_ : 1;
+    nthreads = step_threads(DIM, Exact<R>::value, tx, ty);
     xo = kXo;
     pw = tx + 2 * kXo;
     ph = DIM == 3 ? ty + 4 : 1;
@@ -347,7 +348,7 @@ struct HydroSmem {
     red_off = o;  // reduction scratch
     o += sizeof(double) * 40;
     items_off = o;  // per-thread ring and face work items, packed
-    o += sizeof(int) * (kMaxRingItems + kMaxFaceItems) * tx * ty;
+    o += sizeof(int) * (kMaxRingItems + kMaxFaceItems) * nthreads;
     bytes = ((o + 15) & ~size_t(15)) + 128;  // + room to align the base to 128 bytes
   }
 };
@@ -651,7 +652,7 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   const int ax = min(S.tx, g.na - x0);
   const int by = DIM == 3 ? min(S.ty, g.nb - y0) : 1;
   if (!TFV_IN(12, ax - 1, S.tx) || !TFV_IN(13, by - 1, S.ty) || !TFV_IN(14, p0, p1) ||
-      !TFV_IN(15, p1 - 1, g.np) || !TFV_IN(16, blockDim.x - 1, S.tx * S.ty) ||
+      !TFV_IN(15, p1 - 1, g.np) || !TFV_IN(16, blockDim.x - 1, S.nthreads) ||
       !TFV_IN(17, (int)src, d.nring) || !TFV_IN(18, (int)dst, d.nring))
     return true;
   const int nint = ax * by;
@@ -770,8 +771,11 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   const int NT = blockDim.x;
   constexpr int MR = HydroSmem<R, DIM, VARG>::kMaxRingItems;
   const int nring_cells = DIM == 3 ? 2 * ax + 2 * by : 2;
+  // ring items start at the first lane after the owners when the CTA has
+  // lanes for them (step_threads), else at thread 0
+  const int r0 = NT > S.tx * S.ty ? S.tx * S.ty : 0;
   int n_ritems = 0;
-  for (int q = tid; q < nring_cells + ncorner; q += NT) {
+  for (int q = tid - r0; q >= 0 && q < nring_cells + ncorner; q += NT - r0) {
     int a, b;
     if (q < nring_cells) {
       if (DIM == 3) {
@@ -796,8 +800,9 @@ __device__ bool hydro_tile(const StepArgs& A, int t, unsigned char* smem,
   int n_fitems = 0;
   // the faces do not divide evenly over the threads: the ones that take one
   // more face than the rest start at warp 2, so that they share no warp (and
-  // no scheduler) with the ring cells of warps 0 and 1
-  const int tface = (tid + NT - 64 % NT) % NT;
+  // no scheduler) with the ring cells of warps 0 and 1; with ring lanes after
+  // the owners they start at thread 0
+  const int tface = r0 ? tid : (tid + NT - 64 % NT) % NT;
   for (int w = tface; w < nfa + nfb; w += NT) {
     int packed;
     if (w < nfa) {

@@ -99,4 +99,25 @@ enum : int32_t {
   kFlagChemistry = 8,
 };
 
+// Threads per CTA of the step kernel for a tx x ty tile.  A single-precision
+// tile whose cell count is not a whole number of warps gets the ring cells
+// (2 tx + 2 ty + 4 in 3D, 2 in 2D) on the lanes after its owners, rounded up
+// to whole warps, when that fits 256 threads: each lane then does one cell
+// stage per plane, and no warp a second one before the plane's barrier.
+// Every other tile takes one thread per owned cell.
+#if defined(__CUDACC__)
+#define TFV_HOST_DEVICE __host__ __device__
+#else
+#define TFV_HOST_DEVICE
+#endif
+inline TFV_HOST_DEVICE int step_threads(int dim, bool exact, int tx, int ty) {
+  const int nt = tx * (dim == 3 ? ty : 1);
+  if (!exact && dim >= 2 && nt % 32 != 0) {
+    const int ring = dim == 3 ? 2 * tx + 2 * ty + 4 : 2;
+    const int t = (nt + ring + 31) / 32 * 32;
+    if (t <= 256) return t;
+  }
+  return nt;
+}
+
 }  // namespace tfv
