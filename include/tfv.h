@@ -230,8 +230,9 @@ int tfv_hydro_step(const tfv_config* cfg, int32_t precision, const void* state_i
  * TFV_EINVAL; tfv_step_workspace_size gives a grid's need (with the default
  * tiles a 3D 256^3 grid needs about 376 KiB in fp32 and 856 KiB in fp64, so
  * fp64 3D grids much larger than 256^3 are rejected; a 2D 4096^2 grid needs
- * 856 KiB; 1D tubes need about 49 B per cell in fp32 and 97 B in fp64, so
- * tubes beyond about 21,000 / 10,800 cells are rejected).  The array's device
+ * 456 KiB in fp32 and 856 KiB in fp64; 1D tubes need about 49 B per cell in
+ * fp32 and 97 B in fp64, so tubes beyond about 21,000 / 10,800 cells are
+ * rejected).  The array's device
  * address is looked up (cudaGetSymbolAddress) on every call with the calling
  * thread's device current.  The call blocks until the step has finished (it
  * reads the step's status back to the host), so it cannot be used on a
