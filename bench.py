@@ -628,11 +628,15 @@ def batched_leg(steps=500, count=64, seed=4):
     b.close()
     del b, grids
     seq32 = 0.0
-    for p in prims:  # each grid alone, same tile and graphs
-        g = grid(p, "fp32")
-        s = Batch([g], tile=tile, graph_steps=10)
-        seq32 += _timed(s.stream, lambda: s.advance(steps))
-        s.close()
+    for p in prims:  # each grid alone, graphs, the faster of the default and the batch's tile
+        best = None
+        for t in (None, tile):
+            g = grid(p, "fp32")
+            s = Batch([g], tile=t, graph_steps=10)
+            t_ms = _timed(s.stream, lambda: s.advance(steps))
+            s.close()
+            best = t_ms if best is None else min(best, t_ms)
+        seq32 += best
     seq64, errors = 0.0, []
     for p, u32 in zip(prims, finals):  # plain FP64 alone, every step measured
         g = grid(p, "fp64")
@@ -652,7 +656,8 @@ def batched_leg(steps=500, count=64, seed=4):
         "autotune_s": tune_s,
         "value": upd / (ms * 1e-3), "unit": UNIT, "batch_ms": ms,
         "sequential_fp32": {"value": upd / (seq32 * 1e-3), "ms": seq32,
-                            "how": "each grid alone, all its steps timed"},
+                            "how": "each grid alone, all its steps timed, the faster of the "
+                                   "default tile and the batch's tile"},
         "sequential_fp64_plain": {"value": upd / (seq64 * 1e-3), "ms": seq64,
                                   "how": "each grid alone, all its steps timed"},
         "speedup_vs_sequential_fp32": seq32 / ms,

@@ -652,14 +652,16 @@ static int create_internal(int32_t dim, int32_t precision, int32_t n, const tfv_
     // 3D: 32 x 4 (FP64, one CTA per SM) or 16 x 16 (FP32, three CTAs per SM;
     // the fastest measured shape at 256^3)
     // 2D FP32: rows of 124 cells in 128 threads (the two ring cells on the
-    // spare lanes: no warp does a second cell stage or face per row), 64-row
-    // chunks (4096^2: 32.5 G cell-updates/s against 29.8 for 128 x 32)
+    // spare lanes: no warp does a second cell stage or face per row), 32-row
+    // chunks (4096^2: 31.9 G cell-updates/s against 29.8 for 128 x 32; 64-row
+    // chunks reach 32.5 there but leave small grids too few tiles: the
+    // autotuner tries them per batch)
     const bool f32 = precision == TFV_FP32;
     b->tile.tx = dim == 3 ? (f32 ? 16 : 32) : (dim == 2 ? (f32 ? 124 : 128) : 256);
     b->tile.ty = dim == 3 ? (f32 ? 16 : 4) : 1;
     // 3D FP32: 40-plane chunks (256^3: 1.065 ms per step kernel against 1.105
     // with 32 and 1.085 with 48, measured)
-    b->tile.chunk = dim == 3 && f32 ? 40 : (dim == 2 && f32 ? 64 : 32);
+    b->tile.chunk = dim == 3 && f32 ? 40 : 32;
     b->tile.persistent_ctas = 0;
     b->tile.tma = 1;
   }
