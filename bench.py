@@ -39,7 +39,7 @@ BYTES_PER_CELL = {"fp32": 40, "fp64": 80}  # read + write of 5 conserved values
 # hydro_kernel<float,3,...,16,16> at 192^3 (dram__bytes_read.sum +
 # dram__bytes_write.sum = 152.21 + 108.01 MB for 7,077,888 cells); the traffic
 # grows in proportion to the cells a launch processes.
-TRAFFIC_PER_CELL = (152.21e6 + 108.01e6) / 192 ** 3
+TRAFFIC_PER_CELL = (151.64e6 + 107.19e6) / 192 ** 3
 
 
 def explosion_3d(n, nz=None):
