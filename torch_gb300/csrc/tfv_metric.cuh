@@ -715,6 +715,9 @@ __device__ __forceinline__ int update_cell(const MArgs<R>& A, const MIdx& co, co
   int err = 0;
   const int64_t off = off_of(co.i, co.j, co.k, A.n);
   const R vol = volume<R, DIM>(A, co);
+  // single precision divides by the volume as one reciprocal and products
+  const R ivol = Exact<R>::value ? R(0) : R(1) / vol;
+  auto pv = [&](R x) { return Exact<R>::value ? x / vol : x * ivol; };
   R k[NV], kq[2] = {R(0), R(0)};
 #pragma unroll
   for (int v = 0; v < NV; ++v) k[v] = ro(&A.K[v * A.nc + off]);
@@ -723,17 +726,17 @@ __device__ __forceinline__ int update_cell(const MArgs<R>& A, const MIdx& co, co
   for (int d = 0; d < DIM; ++d) {
     if (d == D) {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) k[v] = k[v] - (whi[v] - wlo[v]) / vol;
+      for (int v = 0; v < NV; ++v) k[v] = k[v] - pv(whi[v] - wlo[v]);
 #pragma unroll
-      for (int q = 0; q < 2; ++q) if (q < A.nfrac) kq[q] = kq[q] - (whi[NV + q] - wlo[NV + q]) / vol;
+      for (int q = 0; q < 2; ++q) if (q < A.nfrac) kq[q] = kq[q] - pv(whi[NV + q] - wlo[NV + q]);
     } else {
       const int64_t lo = face_off(d, cc[d], co, A.n), hi = face_off(d, cc[d] + 1, co, A.n);
       const int64_t nf = A.nf[d];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) k[v] = k[v] - (ro(&A.W[d][v * nf + hi]) - ro(&A.W[d][v * nf + lo])) / vol;
+      for (int v = 0; v < NV; ++v) k[v] = k[v] - pv(ro(&A.W[d][v * nf + hi]) - ro(&A.W[d][v * nf + lo]));
 #pragma unroll
       for (int q = 0; q < 2; ++q) if (q < A.nfrac)
-        kq[q] = kq[q] - (ro(&A.T[d][q * nf + hi]) - ro(&A.T[d][q * nf + lo])) / vol;
+        kq[q] = kq[q] - pv(ro(&A.T[d][q * nf + hi]) - ro(&A.T[d][q * nf + lo]));
     }
   }
   R out[NV], oq[2];
