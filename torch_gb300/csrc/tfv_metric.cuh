@@ -1084,18 +1084,18 @@ __global__ void __launch_bounds__(kMThreads) rusanov_faces_kernel(
 namespace {
 __global__ void __launch_bounds__(256) metric_reduce_kernel(const double* part, int nblocks,
                                                             int nv, double* out) {
-  // the whole CTA stages the partials in shared memory (independent,
-  // coalesced loads), then one thread per component sums them in block
-  // order, the order of a plain sequential sum
-  __shared__ double sp[kMReduceBlocks * 8];
+  // fixed order: thread t sums partials t, t + 256, ...; then the block's
+  // fixed shuffle tree and its warps in order (deterministic, independent of
+  // timing; every partial is loaded by an independent, coalesced load)
+  __shared__ double red[32];
   const int nb = min(nblocks, kMReduceBlocks);
-  for (int e = threadIdx.x; e < nb * 8; e += blockDim.x) sp[e] = part[e];
-  __syncthreads();
-  const int v = threadIdx.x;
-  if (v >= nv) return;
-  double s = 0.0;
-  for (int b = 0; b < nb; ++b) s += sp[b * 8 + v];
-  out[v] = s;
+  for (int v = 0; v < nv; ++v) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += part[b * 8 + v];
+    const double t = block_sum(s, red);
+    if (threadIdx.x == 0) out[v] = t;
+    __syncthreads();  // red is reused by the next component
+  }
 }
 }  // namespace
 
